@@ -1,0 +1,701 @@
+// Host engine of the GB300 PAGANI iteration (see pg_engine.h).
+#include "pg_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+
+namespace pg {
+
+namespace {
+
+inline uint64_t div_up(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+
+inline int parts_for(int d) { return d < 5 ? 4 : (d <= 10 ? 2 : 1); }
+
+inline uint64_t ipow_u(uint64_t b, int e) {
+  uint64_t r = 1;
+  for (int i = 0; i < e; ++i) r *= b;
+  return r;
+}
+
+std::string fixed15(double v) {
+  std::ostringstream out;
+  out.precision(15);
+  out << std::fixed << v;
+  return out.str();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Classifier state (heuristic_classifier.cuh:89-280).
+// ---------------------------------------------------------------------------
+uint64_t ClassifierState::mem_required(uint64_t n) const {
+  // Bytes a full split of n regions needs in the reference's accounting
+  // (heuristic_classifier.cuh:227-264).
+  const uint64_t d = (uint64_t)ndim;
+  const uint64_t doubles = n + n + 2 * n + 2 * n + 2 * n * d + 2 * n * d + n * d * 2 + n * d * 2 + n + n + n * d + n * d;
+  const uint64_t ints = n + 2 * n + n;
+  return 8 * doubles + 4 * ints;
+}
+
+uint64_t ClassifierState::free_mem(uint64_t n) const {
+  const uint64_t total = (uint64_t)total_mem;
+  const uint64_t occ = mem_required(n);
+  return total > occ ? total - occ : 1;
+}
+
+bool ClassifierState::sig_digits_same() const {
+  double third = std::fabs(last[0]), second = std::fabs(last[1]), first = std::fabs(last[2]);
+  while (first != 0. && first < 1.) first *= 10;
+  while (second != 0. && second < 1.) second *= 10;
+  while (third != 0. && third < 1.) third *= 10;
+  const std::string a = fixed15(third), b = fixed15(second), c = fixed15(first);
+  bool verdict = true;
+  int sig = 0;
+  for (int i = 0; i < required_digits + 1 && sig < required_digits && verdict; ++i) {
+    const char ci = i < (int)c.size() ? c[i] : '\0';
+    const char bi = i < (int)b.size() ? b[i] : '\0';
+    const char ai = i < (int)a.size() ? a[i] : '\0';
+    verdict = (ci == bi && bi == ai);
+    sig += (verdict && ci != '.') ? 1 : 0;
+  }
+  return verdict;
+}
+
+bool ClassifierState::estimate_converged() const { return !(iters_collected - 1 < 1 || !sig_digits_same()); }
+
+void ClassifierState::store(double e) {
+  last[0] = last[1];
+  last[1] = last[2];
+  last[2] = e;
+  iters_collected++;
+}
+
+bool ClassifierState::criteria_met(uint64_t n) const {
+  const double ratio = (double)mem_required(n) / (double)free_mem(n);
+  if (ratio > 1.) return true;
+  if (ratio > .1 && estimate_converged()) return true;
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+int prepare_desc(const pg_integrand& f, const double* lows, const double* highs, IntegralDesc* out,
+                 std::string* why) {
+  if (f.ndim < PG_MIN_NDIM || f.ndim > kMaxNdim) {
+    if (why) *why = "ndim out of range";
+    return PG_BAD_ARG;
+  }
+  if (f.family < 0 || f.family >= FAM_COUNT) {
+    if (why) *why = "unknown integrand family";
+    return PG_BAD_ARG;
+  }
+  if (f.family == FAM_FUN6 && f.ndim != 6) {
+    if (why) *why = "FUN6 is a 6-dimensional integrand";
+    return PG_BAD_ARG;
+  }
+  IntegralDesc D;
+  std::memset(&D, 0, sizeof D);
+  D.family = f.family;
+  D.d = f.ndim;
+  D.c = f.c;
+  D.s0 = 2.0 * 3.14159265358979323846 * f.u[0];
+  if (f.family == FAM_FUN6) D.c = 12.0 / (7.0 - 6.0 * std::log(2.0) * std::log(2.0) + std::log(64.0));
+  D.jac = 1.0;
+  int unit = 1;
+  for (int k = 0; k < kMaxDim; ++k) {
+    D.a[k] = f.a[k];
+    D.u[k] = f.u[k];
+    D.ia2[k] = 1.0 / (f.a[k] * f.a[k]);
+  }
+  for (int k = 0; k < f.ndim; ++k) {
+    const double lo = lows ? lows[k] : 0.0, hi = highs ? highs[k] : 1.0;
+    if (!(hi > lo) || !std::isfinite(lo) || !std::isfinite(hi)) {
+      if (why) *why = "each axis needs finite bounds with low < high";
+      return PG_BAD_ARG;
+    }
+    D.glo[k] = lo;
+    D.range[k] = hi - lo;
+    D.jac = D.jac * D.range[k];
+    if (lo != 0.0 || D.range[k] != 1.0) unit = 0;
+  }
+  D.unit = unit;
+  *out = D;
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+Engine::Engine(int dev) : device(dev) {}
+
+Engine::~Engine() {
+  cudaSetDevice(device);
+  DevBuf* dev_bufs[] = {&rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
+                        &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
+                        &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
+                        &thr_out_};
+  for (DevBuf* b : dev_bufs)
+    if (b->p) cudaFree(b->p);
+  DevBuf* host_bufs[] = {&h_segs_, &h_chunks_, &h_trans_, &h_scal_, &h_live_, &h_thr_};
+  for (DevBuf* b : host_bufs)
+    if (b->p) cudaFreeHost(b->p);
+  for (auto& e : ev_)
+    if (e) cudaEventDestroy(e);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Engine::fail(cudaError_t e, const char* what) {
+  last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return PG_OOM;
+  return PG_CUDA_ERROR;
+}
+
+#define PG_TRY(call, what)                  \
+  do {                                      \
+    cudaError_t e_ = (call);                \
+    if (e_ != cudaSuccess) return fail(e_, what); \
+  } while (0)
+
+int Engine::ensure(DevBuf& b, size_t bytes) {
+  if (b.bytes >= bytes) return PG_OK;
+  // Kernels queued on the stream may still read the old buffer.
+  if (stream_) PG_TRY(cudaStreamSynchronize(stream_), "stream sync before reallocation");
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  size_t want = std::max(bytes, (size_t)4096);
+  PG_TRY(cudaMalloc(&b.p, want), "cudaMalloc");
+  b.bytes = want;
+  return PG_OK;
+}
+
+int Engine::ensure_pinned(DevBuf& b, size_t bytes) {
+  if (b.bytes >= bytes) return PG_OK;
+  if (stream_) PG_TRY(cudaStreamSynchronize(stream_), "stream sync before reallocation");
+  if (b.p) cudaFreeHost(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  size_t want = std::max(bytes, (size_t)4096);
+  PG_TRY(cudaMallocHost(&b.p, want), "cudaMallocHost");
+  b.bytes = want;
+  return PG_OK;
+}
+
+int Engine::init(std::string* why) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    if (why) *why = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return PG_CUDA_ERROR;
+  }
+  int rc;
+#define PG_INIT_TRY(call, what)                                                     \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      if (why) *why = std::string(what) + ": " + cudaGetErrorString(e_);            \
+      return e_ == cudaErrorMemoryAllocation ? PG_OOM : PG_CUDA_ERROR;              \
+    }                                                                               \
+  } while (0)
+  PG_INIT_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  PG_INIT_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+  for (auto& ev : ev_) PG_INIT_TRY(cudaEventCreate(&ev), "cudaEventCreate");
+  // Rule tables for every supported ndim.
+  std::vector<uint64_t> codes;
+  std::vector<double> w((kMaxNdim + 1) * 45, 0.0), sc((kMaxNdim + 1) * 45, 0.0), nm((kMaxNdim + 1) * 45, 0.0);
+  RuleDev R;
+  std::memset(&R, 0, sizeof R);
+  RuleTable r2;
+  for (int d = PG_MIN_NDIM; d <= kMaxNdim; ++d) {
+    RuleTable t = make_rule(d);
+    R.code_off[d] = (int32_t)codes.size();
+    R.feval[d] = t.feval;
+    codes.insert(codes.end(), t.code.begin(), t.code.end());
+    std::memcpy(&w[d * 45], t.w, sizeof t.w);
+    std::memcpy(&sc[d * 45], t.scale, sizeof t.scale);
+    std::memcpy(&nm[d * 45], t.norm, sizeof t.norm);
+    if (d == PG_MIN_NDIM) r2 = t;
+  }
+  code_coefficients(r2, R.A, R.B);
+  const double q = r2.G[1] / r2.G[0];
+  R.ratio = q * q;
+  if ((rc = ensure(rule_code_, codes.size() * 8)) != PG_OK) {
+    if (why) *why = last_error;
+    return rc;
+  }
+  if ((rc = ensure(rule_w_, w.size() * 8)) != PG_OK || (rc = ensure(rule_scale_, sc.size() * 8)) != PG_OK ||
+      (rc = ensure(rule_norm_, nm.size() * 8)) != PG_OK) {
+    if (why) *why = last_error;
+    return rc;
+  }
+  PG_INIT_TRY(cudaMemcpy(rule_code_.p, codes.data(), codes.size() * 8, cudaMemcpyHostToDevice), "rule upload");
+  PG_INIT_TRY(cudaMemcpy(rule_w_.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice), "rule upload");
+  PG_INIT_TRY(cudaMemcpy(rule_scale_.p, sc.data(), sc.size() * 8, cudaMemcpyHostToDevice), "rule upload");
+  PG_INIT_TRY(cudaMemcpy(rule_norm_.p, nm.data(), nm.size() * 8, cudaMemcpyHostToDevice), "rule upload");
+  R.code = (const uint64_t*)rule_code_.p;
+  R.w = (const double*)rule_w_.p;
+  R.scale = (const double*)rule_scale_.p;
+  R.norm = (const double*)rule_norm_.p;
+  rule_ = R;
+  if ((rc = ensure(thr_out_, 64)) != PG_OK || (rc = ensure_pinned(h_thr_, 64)) != PG_OK) {
+    if (why) *why = last_error;
+    return rc;
+  }
+#undef PG_INIT_TRY
+  return PG_OK;
+}
+
+void Engine::record(cudaEvent_t a, cudaEvent_t b, double* acc) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) *acc += ms;
+}
+
+int Engine::evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length,
+                     uint64_t stride, double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch) {
+  int rc;
+  if ((rc = ensure(descs_, sizeof(IntegralDesc))) != PG_OK) return rc;
+  PG_TRY(cudaMemcpyAsync(descs_.p, &desc, sizeof desc, cudaMemcpyHostToDevice, stream_), "desc upload");
+  if (n == 0) return PG_OK;
+  EvalLaunch L{d_left, d_length, n, stride, nullptr, (const IntegralDesc*)descs_.p, &rule_, d_est, d_err, d_bisect,
+               desc.d, num_sms, stream_};
+  if (profiling) cudaEventRecord(ev_[0], stream_);
+  PG_TRY(launch(L), "evaluation launch");
+  stats.launches++;
+  stats.eval_launches++;
+  stats.regions_evaluated += n;
+  stats.points_evaluated += n * (uint64_t)rule_.feval[desc.d];
+  if (profiling) {
+    cudaEventRecord(ev_[1], stream_);
+    PG_TRY(cudaEventSynchronize(ev_[1]), "evaluation");
+    record(ev_[0], ev_[1], &stats.eval_ms);
+  }
+  return PG_OK;
+}
+
+// One pass of the threshold kernels over integral jidx's chunks; out = {sum
+// err*flag, sum est*flag, count, min err, max err}.
+int Engine::threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5]) {
+  const SegDesc& S = ((const SegDesc*)h_segs_.p)[jidx];
+  if (S.nchunks) {
+    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>((const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p,
+                                                             S.chunk_start, (const double*)est_.p,
+                                                             (const double*)err_b_.p, thr, write_flags, minmax,
+                                                             (uint8_t*)active_.p, (Partial*)partials_.p);
+    stats.launches++;
+  }
+  threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>((const SegDesc*)segs_.p, jidx,
+                                                            (const Partial*)partials_.p, (uint64_t*)chunk_off_.p,
+                                                            scan, (double*)thr_out_.p);
+  stats.launches++;
+  PG_TRY(cudaGetLastError(), "threshold launch");
+  PG_TRY(cudaMemcpyAsync(h_thr_.p, thr_out_.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+         "threshold readback");
+  PG_TRY(cudaStreamSynchronize(stream_), "threshold pass");
+  std::memcpy(out, h_thr_.p, 5 * sizeof(double));
+  stats.d2h_bytes += 5 * sizeof(double);
+  return PG_OK;
+}
+
+// Memory-pressure classification of one integral (heuristic_classifier.cuh:362-451,
+// Workspace.cuh:74-118).  On success the integral's active flags and chunk
+// offsets are rewritten for the threshold found.
+int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err, bool* ok_out, double* fin_est_out,
+                         double* fin_err_out, uint64_t* num_active_out, double iter_est) {
+  ClassifierState& C = J.cls;
+  const uint64_t n = J.n;
+  double o[5];
+  int rc;
+  if ((rc = threshold_pass(jidx, INFINITY, 0, 1, 0, o)) != PG_OK) return rc;
+  const double mn = o[3], mx = o[4];
+  double low = mn, high = mx, thr = iter_err / (double)n, flags_thr = thr;
+  bool pass_mem = false, pass_budget = false;
+  uint64_t num_active = 0;
+  double dot_err = 0, dot_est = 0, finished_errorest = 0;
+  const double target = std::fabs(C.last[2]) * C.epsrel;
+  uint64_t inc = 0, dec = 0;
+  auto apply = [&](double t) -> int {
+    double q[5];
+    int r2 = threshold_pass(jidx, t, 0, 0, 0, q);
+    if (r2 != PG_OK) return r2;
+    flags_thr = t;
+    dot_err = q[0];
+    dot_est = q[1];
+    num_active = (uint64_t)q[2];
+    const double pct = (double)(int)num_active / (double)(int)n;
+    pass_mem = pct <= C.max_active_regions_percentage;
+    return PG_OK;
+  };
+  do {
+    if (!pass_mem && inc <= 20) {
+      pass_mem = false;
+      for (uint64_t cnt = 0; !pass_mem && cnt < 20; ++cnt) {
+        if ((rc = apply(thr)) != PG_OK) return rc;
+        if (!pass_mem) {
+          low = thr;
+          thr += std::fabs(high - thr) * .5;
+        }
+      }
+      inc++;
+    }
+    if (pass_mem) {
+      const double extra = iter_err - dot_err - fin_err;
+      const double budget = target - J.res.errorest;
+      pass_budget = extra <= C.max_percent_error_budget * budget;
+      finished_errorest = extra;
+      if (!pass_budget && dec <= 20) {
+        high = thr;
+        thr -= std::fabs(low - thr) * .5;
+        pass_mem = false;
+        dec++;
+      }
+    }
+    const bool exhausted = dec >= 20 || inc >= 20;
+    if (exhausted && C.max_percent_error_budget < .7) {
+      C.max_percent_error_budget += 0.1;
+      dec = inc = 0;
+      low = mn;
+      high = mx;
+      thr = iter_err / (double)n;
+    } else if (exhausted && C.max_percent_error_budget >= .7 && C.max_active_regions_percentage <= .7) {
+      C.max_active_regions_percentage += .1;
+    } else if (exhausted) {
+      break;
+    }
+  } while (!pass_mem || !pass_budget);
+  C.max_active_regions_percentage = .5;
+  C.max_percent_error_budget = .25;
+  const bool ok = pass_mem && pass_budget;
+  *ok_out = ok;
+  *num_active_out = num_active;
+  if (ok) {
+    if ((rc = threshold_pass(jidx, flags_thr, 1, 0, 1, o)) != PG_OK) return rc;
+    *fin_est_out = iter_est - dot_est;
+    *fin_err_out = finished_errorest;
+  }
+  return PG_OK;
+}
+
+int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch) {
+  int rc;
+  PG_TRY(cudaSetDevice(device), "cudaSetDevice");
+  const uint32_t njobs = (uint32_t)jobs.size();
+  if (njobs == 0) return PG_OK;
+  int maxd = 2;
+  for (auto& J : jobs) maxd = std::max(maxd, J.desc.d);
+  // Per-integral arrays.
+  if ((rc = ensure(descs_, njobs * sizeof(IntegralDesc))) != PG_OK) return rc;
+  if ((rc = ensure(segs_, njobs * sizeof(SegDesc))) != PG_OK) return rc;
+  if ((rc = ensure(trans_, njobs * sizeof(Transition))) != PG_OK) return rc;
+  if ((rc = ensure(scal_, njobs * sizeof(IterScalars))) != PG_OK) return rc;
+  if ((rc = ensure(live_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_segs_, njobs * sizeof(SegDesc))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_trans_, njobs * sizeof(Transition))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_scal_, njobs * sizeof(IterScalars))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_live_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
+  {
+    std::vector<IntegralDesc> descs(njobs);
+    for (uint32_t j = 0; j < njobs; ++j) descs[j] = jobs[j].desc;
+    PG_TRY(cudaMemcpyAsync(descs_.p, descs.data(), njobs * sizeof(IntegralDesc), cudaMemcpyHostToDevice, stream_),
+           "desc upload");
+    PG_TRY(cudaStreamSynchronize(stream_), "desc upload");
+    stats.h2d_bytes += njobs * sizeof(IntegralDesc);
+  }
+  // Initial uniform split of every integral, one launch for the batch.
+  uint64_t total = 0;
+  {
+    uint64_t* starts = (uint64_t*)h_live_.p;
+    for (uint32_t j = 0; j < njobs; ++j) {
+      Job& J = jobs[j];
+      J.res = pg_result{};
+      J.res.status = 1;
+      J.res.last_phase = -1;
+      J.cls = ClassifierState{};
+      J.cls.epsrel = J.epsrel;
+      J.cls.epsabs = J.epsabs;
+      J.cls.required_digits = (int)std::ceil(std::log10(1 / J.epsrel));
+      J.cls.ndim = J.desc.d;
+      J.cls.total_mem = J.opt.device_mem_model > 0 ? J.opt.device_mem_model : 16e9;
+      J.n = ipow_u((uint64_t)parts_for(J.desc.d), J.desc.d);
+      J.start = total;
+      J.par_start = 0;
+      J.has_parent = 0;
+      J.iters = 0;
+      J.done = false;
+      starts[j] = total;
+      total += J.n;
+    }
+    starts[njobs] = total;
+    if ((rc = ensure(left_[0], total * maxd * 8)) != PG_OK) return rc;
+    if ((rc = ensure(len_[0], total * maxd * 8)) != PG_OK) return rc;
+    if ((rc = ensure(owner_[0], total * 4)) != PG_OK) return rc;
+    reg_cap_[0] = left_[0].bytes / (maxd * 8);
+    reg_cap_[0] = std::min(reg_cap_[0], len_[0].bytes / (maxd * 8));
+    reg_rows_[0] = maxd;
+    PG_TRY(cudaMemcpyAsync(live_.p, starts, (njobs + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, stream_),
+           "start upload");
+    uniform_split_batch_kernel<<<(unsigned)div_up(total, 256), 256, 0, stream_>>>(
+        (double*)left_[0].p, (double*)len_[0].p, reg_cap_[0], (uint32_t*)owner_[0].p, (const uint64_t*)live_.p,
+        (const IntegralDesc*)descs_.p, njobs);
+    stats.launches++;
+    PG_TRY(cudaGetLastError(), "uniform split launch");
+    PG_TRY(cudaStreamSynchronize(stream_), "uniform split");
+  }
+  int cur = 0;
+  std::vector<uint32_t> live;
+  std::vector<ChunkRef> chunk_list;
+  std::vector<int> mode(njobs);
+  std::vector<uint64_t> keepA(njobs);
+  while (true) {
+    live.clear();
+    for (uint32_t j = 0; j < njobs; ++j)
+      if (!jobs[j].done) live.push_back(j);
+    if (live.empty()) break;
+    // Segments and chunk list of the live integrals.
+    chunk_list.clear();
+    SegDesc* hs = (SegDesc*)h_segs_.p;
+    uint64_t N = 0;
+    for (uint32_t j = 0; j < njobs; ++j) {
+      Job& J = jobs[j];
+      SegDesc S;
+      std::memset(&S, 0, sizeof S);
+      S.start = J.start;
+      S.n = J.done ? 0 : J.n;
+      S.par_start = J.par_start;
+      S.chunk_start = (uint32_t)chunk_list.size();
+      S.nchunks = (uint32_t)div_up(S.n, kChunk);
+      S.has_parent = J.has_parent;
+      S.relerr = J.opt.relerr_classification;
+      S.epsrel = J.epsrel;
+      for (uint32_t b = 0; b < S.nchunks; ++b) chunk_list.push_back(ChunkRef{j, b});
+      hs[j] = S;
+      if (!J.done) N = std::max(N, J.start + J.n);
+    }
+    const uint64_t nchunks = chunk_list.size();
+    if ((rc = ensure(est_, N * 8)) != PG_OK) return rc;
+    if ((rc = ensure(err_a_, N * 8)) != PG_OK) return rc;
+    if ((rc = ensure(err_b_, N * 8)) != PG_OK) return rc;
+    if ((rc = ensure(bisect_, N * 4)) != PG_OK) return rc;
+    if ((rc = ensure(active_, N)) != PG_OK) return rc;
+    if ((rc = ensure(partials_, nchunks * sizeof(Partial))) != PG_OK) return rc;
+    if ((rc = ensure(chunk_off_, nchunks * 8)) != PG_OK) return rc;
+    if ((rc = ensure(chunks_, nchunks * sizeof(ChunkRef))) != PG_OK) return rc;
+    if ((rc = ensure_pinned(h_chunks_, nchunks * sizeof(ChunkRef))) != PG_OK) return rc;
+    std::memcpy(h_chunks_.p, chunk_list.data(), nchunks * sizeof(ChunkRef));
+    uint32_t* hl = (uint32_t*)h_live_.p;
+    for (size_t q = 0; q < live.size(); ++q) hl[q] = live[q];
+    PG_TRY(cudaMemcpyAsync(segs_.p, hs, njobs * sizeof(SegDesc), cudaMemcpyHostToDevice, stream_), "seg upload");
+    PG_TRY(cudaMemcpyAsync(chunks_.p, h_chunks_.p, nchunks * sizeof(ChunkRef), cudaMemcpyHostToDevice, stream_),
+           "chunk upload");
+    PG_TRY(cudaMemcpyAsync(live_.p, hl, live.size() * 4, cudaMemcpyHostToDevice, stream_), "live upload");
+    stats.h2d_bytes += njobs * sizeof(SegDesc) + nchunks * sizeof(ChunkRef) + live.size() * 4;
+    // 1. evaluation
+    EvalLaunch L{(const double*)left_[cur].p, (const double*)len_[cur].p, N, reg_cap_[cur],
+                 (const uint32_t*)owner_[cur].p, (const IntegralDesc*)descs_.p, &rule_, (double*)est_.p,
+                 (double*)err_a_.p, (int32_t*)bisect_.p, maxd, num_sms, stream_};
+    if (profiling) cudaEventRecord(ev_[0], stream_);
+    PG_TRY(launch(L), "evaluation launch");
+    stats.launches++;
+    stats.eval_launches++;
+    stats.regions_evaluated += N;
+    for (uint32_t j : live) stats.points_evaluated += jobs[j].n * (uint64_t)rule_.feval[jobs[j].desc.d];
+    if (profiling) cudaEventRecord(ev_[1], stream_);
+    // 2. two-level error + classification + partial sums; 3. per-integral totals
+    two_level_kernel<<<(unsigned)nchunks, kRedThreads, 0, stream_>>>(
+        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const double*)est_.p, (const double*)err_a_.p,
+        (const double*)parent_[cur].p, (double*)err_b_.p, (uint8_t*)active_.p, (Partial*)partials_.p);
+    finalize_kernel<<<(unsigned)live.size(), kRedThreads, 0, stream_>>>(
+        (const uint32_t*)live_.p, (const SegDesc*)segs_.p, (const Partial*)partials_.p, (uint64_t*)chunk_off_.p,
+        (IterScalars*)scal_.p);
+    stats.launches += 2;
+    PG_TRY(cudaGetLastError(), "two-level launch");
+    if (profiling) cudaEventRecord(ev_[2], stream_);
+    PG_TRY(cudaMemcpyAsync(h_scal_.p, scal_.p, njobs * sizeof(IterScalars), cudaMemcpyDeviceToHost, stream_),
+           "scalar readback");
+    PG_TRY(cudaStreamSynchronize(stream_), "iteration");
+    stats.d2h_bytes += njobs * sizeof(IterScalars);
+    stats.stage_bytes += N * 29;
+    if (profiling) {
+      record(ev_[0], ev_[1], &stats.eval_ms);
+      record(ev_[1], ev_[2], &stats.stage_ms);
+    }
+    const IterScalars* sc = (const IterScalars*)h_scal_.p;
+    // Host decisions, per integral, exactly as Workspace::integrate.
+    for (uint32_t j : live) {
+      Job& J = jobs[j];
+      pg_result& cum = J.res;
+      const IterScalars S = sc[j];
+      const uint64_t n = J.n;
+      cum.neval += n * (uint64_t)rule_.feval[J.desc.d];
+      mode[j] = 0;
+      keepA[j] = 0;
+      const double iter_est = S.iter_est, iter_err = S.iter_err;
+      const double cest = std::fabs(cum.estimate + iter_est), cerr = cum.errorest + iter_err;
+      J.iters++;
+      if (cerr / cest <= J.epsrel || cerr <= J.epsabs) {  // accuracy_reached (PaganiUtils.cuh:387-394)
+        cum.estimate += iter_est;
+        cum.errorest += iter_err;
+        cum.status = 0;
+        cum.nregions += n;
+        J.done = true;
+        continue;
+      }
+      J.cls.store(cum.estimate + iter_est);
+      double fin_est = iter_est - S.act_est;
+      double fin_err = iter_err - S.act_err;
+      int m = 1;
+      uint64_t A = S.active;
+      // fix_error_budget_overflow (Workspace.cuh:121-146)
+      if (cum.errorest + fin_err > std::fabs(cum.estimate + iter_est) * J.epsrel) {
+        m = 2;
+        A = n;
+        fin_err = 0.;
+        fin_est = 0.;
+      }
+      // heuristic_classify (Workspace.cuh:74-118)
+      bool must_terminate;
+      {
+        const double ratio = (double)J.cls.mem_required(n) / (double)J.cls.free_mem(n);
+        const bool necessary = ratio > 1.;
+        if (!J.cls.criteria_met(n)) {
+          must_terminate = necessary;
+        } else {
+          bool ok = false;
+          uint64_t na = 0;
+          double fe = fin_est, fr = fin_err;
+          if ((rc = classify_job(J, j, iter_err, fin_err, &ok, &fe, &fr, &na, iter_est)) != PG_OK) return rc;
+          if (ok) {
+            m = 1;
+            A = na;
+            fin_est = fe;
+            fin_err = fr;
+          }
+          must_terminate = (!ok && necessary) || na == 0;
+        }
+      }
+      if (must_terminate) {
+        cum.estimate += iter_est;
+        cum.errorest += iter_err;
+        cum.nregions += n;
+        J.done = true;
+        continue;
+      }
+      cum.estimate += fin_est;
+      cum.errorest += fin_err;
+      cum.nregions += n - A;
+      cum.nfinished += n - A;
+      cum.iters++;
+      if (A == 0) {
+        J.done = true;
+        continue;
+      }
+      if (J.iters >= J.opt.max_iters) {  // loop cap: the split list is counted, never evaluated
+        cum.nregions += 2 * A;
+        J.done = true;
+        continue;
+      }
+      mode[j] = m;
+      keepA[j] = A;
+    }
+    // Layout of the next list.
+    Transition* ht = (Transition*)h_trans_.p;
+    uint64_t out_total = 0, par_total = 0;
+    for (uint32_t j = 0; j < njobs; ++j) {
+      Transition T;
+      std::memset(&T, 0, sizeof T);
+      const bool go = !jobs[j].done && mode[j] != 0;
+      if (go) {
+        T.mode = mode[j];
+        T.A = keepA[j];
+        T.out_start = out_total;
+        T.par_out = par_total;
+        out_total += 2 * keepA[j];
+        par_total += keepA[j];
+      }
+      ht[j] = T;
+    }
+    if (out_total == 0) continue;  // every integral finished this iteration
+    const int nxt = cur ^ 1;
+    if (reg_cap_[nxt] < out_total || reg_rows_[nxt] < maxd) {
+      const uint64_t cap = std::max<uint64_t>(out_total + out_total / 2, 1024);
+      PG_TRY(cudaStreamSynchronize(stream_), "stream sync before reallocation");
+      if (left_[nxt].p) cudaFree(left_[nxt].p), left_[nxt] = DevBuf{};
+      if (len_[nxt].p) cudaFree(len_[nxt].p), len_[nxt] = DevBuf{};
+      if ((rc = ensure(left_[nxt], cap * maxd * 8)) != PG_OK) return rc;
+      if ((rc = ensure(len_[nxt], cap * maxd * 8)) != PG_OK) return rc;
+      reg_cap_[nxt] = cap;
+      reg_rows_[nxt] = maxd;
+    }
+    if ((rc = ensure(owner_[nxt], out_total * 4)) != PG_OK) return rc;
+    if ((rc = ensure(parent_[nxt], par_total * 8)) != PG_OK) return rc;
+    PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
+           "transition upload");
+    stats.h2d_bytes += njobs * sizeof(Transition);
+    if (profiling) cudaEventRecord(ev_[2], stream_);
+    const uint64_t out_stride = reg_cap_[nxt];
+    if (maxd <= 8) {
+      compact_split_kernel<8><<<(unsigned)nchunks, kRedThreads, 0, stream_>>>(
+          (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
+          (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
+          (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
+          (const double*)est_.p, (double*)left_[nxt].p, (double*)len_[nxt].p, out_stride, (uint32_t*)owner_[nxt].p,
+          (double*)parent_[nxt].p);
+    } else {
+      compact_split_kernel<16><<<(unsigned)nchunks, kRedThreads, 0, stream_>>>(
+          (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
+          (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
+          (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
+          (const double*)est_.p, (double*)left_[nxt].p, (double*)len_[nxt].p, out_stride, (uint32_t*)owner_[nxt].p,
+          (double*)parent_[nxt].p);
+    }
+    stats.launches++;
+    PG_TRY(cudaGetLastError(), "compact/split launch");
+    if (profiling) {
+      cudaEventRecord(ev_[3], stream_);
+      PG_TRY(cudaEventSynchronize(ev_[3]), "compact/split");
+      record(ev_[2], ev_[3], &stats.stage_ms);
+    }
+    for (uint32_t j = 0; j < njobs; ++j) {
+      const Transition& T = ht[j];
+      if (jobs[j].done || T.mode == 0) continue;
+      Job& J = jobs[j];
+      stats.stage_bytes += J.n + T.A * (uint64_t)(16 * J.desc.d + 12) + 2 * T.A * (uint64_t)(16 * J.desc.d + 4) +
+                           T.A * 8;
+      J.start = T.out_start;
+      J.n = 2 * T.A;
+      J.par_start = T.par_out;
+      J.has_parent = 1;
+    }
+    cur = nxt;
+  }
+  PG_TRY(cudaStreamSynchronize(stream_), "run");
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation launcher for the C ABI families.
+// ---------------------------------------------------------------------------
+template <int MAXD>
+static cudaError_t launch_family_eval_t(const EvalLaunch& L) {
+  const size_t smem = sizeof(EvalWarpSmem<MAXD>) * kEvalWarps;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(eval_kernel<MAXD, FamilyFn>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const uint64_t want = div_up(L.n, kEvalWarps);
+  const uint64_t cap = (uint64_t)L.num_sms * 32;
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+  eval_kernel<MAXD, FamilyFn><<<grid, kEvalWarps * 32, smem, L.stream>>>(
+      L.left, L.length, L.n, L.stride, L.owner, L.descs, *L.rule, FamilyFn{}, L.est, L.err, L.bisect);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_family_eval(const EvalLaunch& L) {
+  if (L.maxd <= 8) return launch_family_eval_t<8>(L);
+  return launch_family_eval_t<16>(L);
+}
+
+}  // namespace pg

@@ -1,0 +1,139 @@
+// Host engine of the GB300 PAGANI iteration.
+//
+// One engine runs any number of integrals together (a batch of one is the
+// plain per-call path).  Each integral follows exactly the reference's
+// Workspace::integrate loop (cuda/pagani/quad/GPUquad/Workspace.cuh:361-494);
+// the integrals only share the device region list and the kernel launches, so
+// an integral's result is bit-identical whether it runs alone or in a batch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "../../include/pagani_gb300.h"
+#include "pg_kernels.cuh"
+#include "pg_rule.h"
+
+namespace pg {
+
+// Arguments of one evaluation launch.
+struct EvalLaunch {
+  const double* left;
+  const double* length;
+  uint64_t n;
+  uint64_t stride;
+  const uint32_t* owner;
+  const IntegralDesc* descs;
+  const RuleDev* rule;
+  double* est;
+  double* err;
+  int32_t* bisect;
+  int maxd;
+  int num_sms;
+  cudaStream_t stream;
+};
+
+// Launches the evaluation kernel for some integrand functor type.
+using EvalLauncher = std::function<cudaError_t(const EvalLaunch&)>;
+
+// The launcher of the C ABI families.
+cudaError_t launch_family_eval(const EvalLaunch& L);
+
+// Host mirror of the memory-pressure classifier's state
+// (heuristic_classifier.cuh:147-225).
+struct ClassifierState {
+  double epsrel = 0, epsabs = 0;
+  int required_digits = 0;
+  double last[3] = {0, 0, 0};
+  uint64_t iters_collected = 0;
+  double max_percent_error_budget = .25;
+  double max_active_regions_percentage = .5;
+  double total_mem = 16e9;
+  int ndim = 0;
+
+  uint64_t mem_required(uint64_t n) const;
+  uint64_t free_mem(uint64_t n) const;
+  bool sig_digits_same() const;
+  bool estimate_converged() const;
+  void store(double e);
+  bool criteria_met(uint64_t n) const;
+};
+
+struct Job {
+  IntegralDesc desc{};
+  double epsrel = 1e-3, epsabs = 1e-12;
+  pg_options opt{};
+  ClassifierState cls;
+  pg_result res{};
+  uint64_t n = 0;      // regions in the current list
+  uint64_t start = 0;  // first region in the current list
+  uint64_t par_start = 0;
+  int has_parent = 0;
+  int iters = 0;
+  bool done = false;
+  int error = 0;
+};
+
+// Prepares an IntegralDesc from the C ABI description (host, no contraction).
+int prepare_desc(const pg_integrand& f, const double* lows, const double* highs, IntegralDesc* out, std::string* why);
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+class Engine {
+ public:
+  explicit Engine(int device);
+  ~Engine();
+  int init(std::string* why);
+
+  // Runs every job to completion.  Returns PG_OK or a negative pg_status.
+  int run(std::vector<Job>& jobs, const EvalLauncher& launch);
+
+  // Evaluates caller-given regions (device pointers, SoA stride n).
+  int evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length, uint64_t stride,
+               double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch);
+
+  cudaStream_t stream() const { return stream_; }
+  const RuleDev& rule() const { return rule_; }
+  pg_stats stats{};
+  bool profiling = false;
+  std::string last_error;
+  int device = 0;
+  int num_sms = 152;
+
+  // Device scratch helpers (grow-only).
+  int ensure(DevBuf& b, size_t bytes);
+  int ensure_pinned(DevBuf& b, size_t bytes);
+
+ private:
+  int fail(cudaError_t e, const char* what);
+  int classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err, bool* ok, double* fin_est_out,
+                   double* fin_err_out, uint64_t* num_active, double iter_est);
+  int threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5]);
+  void record(cudaEvent_t a, cudaEvent_t b, double* acc);
+
+  cudaStream_t stream_ = nullptr;
+  RuleDev rule_{};
+  DevBuf rule_code_, rule_w_, rule_scale_, rule_norm_;
+  // region lists (ping-pong) and owners
+  DevBuf left_[2], len_[2], owner_[2], parent_[2];
+  uint64_t reg_cap_[2] = {0, 0};
+  int reg_rows_[2] = {0, 0};
+  // per-region scratch
+  DevBuf est_, err_a_, err_b_, bisect_, active_;
+  // per-chunk
+  DevBuf partials_, chunk_off_, chunks_;
+  // per-integral
+  DevBuf segs_, trans_, descs_, scal_, live_, thr_out_;
+  // pinned host mirrors
+  DevBuf h_segs_, h_chunks_, h_trans_, h_scal_, h_live_, h_thr_;
+  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+}  // namespace pg

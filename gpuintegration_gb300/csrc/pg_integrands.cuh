@@ -1,0 +1,155 @@
+// Integrand families of the C ABI, evaluated on the device.
+//
+// A device functor cannot cross a C ABI, so C callers name an integrand by
+// family and parameters (pg_integrand).  Every family is written with explicit
+// IEEE operations (__dadd_rn, __fma_rn, ...) in a fixed order so that the CPU
+// oracle, which spells out the same operations, reproduces the values
+// exactly for the families built from +, -, *, / alone.
+#pragma once
+
+#include <stdint.h>
+
+#include "pg_common.cuh"
+
+namespace pg {
+
+enum Family : int32_t {
+  FAM_CONSTANT = 0,
+  FAM_OSCILLATORY = 1,
+  FAM_PRODUCT_PEAK = 2,
+  FAM_CORNER_PEAK = 3,
+  FAM_GAUSSIAN = 4,
+  FAM_C0 = 5,
+  FAM_DISCONTINUOUS = 6,
+  FAM_PRODUCT = 7,
+  FAM_NAN = 8,
+  FAM_BOX = 9,
+  FAM_FUN6 = 10,
+  FAM_COUNT = 11
+};
+
+// Everything a kernel needs to know about one integral: its integrand, the
+// integration box and derived constants.  Prepared on the host once per call.
+struct IntegralDesc {
+  int32_t family;
+  int32_t d;
+  int32_t unit;  // 1 when the box is [0,1]^d: the final x = lo + t*range is then exactly t
+  int32_t pad;
+  double jac;    // product of the box's side lengths (Phases.cuh:329-348)
+  double c;
+  double s0;
+  double glo[kMaxDim];
+  double range[kMaxDim];
+  double a[kMaxDim];
+  double u[kMaxDim];
+  double ia2[kMaxDim];  // 1 / a_i^2 (product peak)
+};
+
+__device__ __forceinline__ double ipow_dev(double s, int e) {
+  double r = 1.0, b = s;
+  while (e) {
+    if (e & 1) r = __dmul_rn(r, b);
+    e >>= 1;
+    if (e) b = __dmul_rn(b, b);
+  }
+  return r;
+}
+
+template <int MAXD>
+__device__ __forceinline__ double family_eval(const IntegralDesc& D, const double* x) {
+  const int d = D.d;
+  switch (D.family) {
+    case FAM_CONSTANT:
+      return D.c;
+    case FAM_OSCILLATORY: {
+      double s = D.s0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i)
+        if (i < d) s = __fma_rn(D.a[i], x[i], s);
+      return cos(s);
+    }
+    case FAM_PRODUCT_PEAK: {
+      double v = 1.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i) {
+        if (i < d) {
+          const double t = __dsub_rn(x[i], D.u[i]);
+          const double term = __ddiv_rn(1.0, __fma_rn(t, t, D.ia2[i]));
+          v = (i == 0) ? term : __dmul_rn(v, term);
+        }
+      }
+      return v;
+    }
+    case FAM_CORNER_PEAK: {
+      double s = 1.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i)
+        if (i < d) s = __fma_rn(D.a[i], x[i], s);
+      return __ddiv_rn(1.0, ipow_dev(s, d + 1));
+    }
+    case FAM_GAUSSIAN: {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i) {
+        if (i < d) {
+          const double q = __dmul_rn(D.a[i], __dsub_rn(x[i], D.u[i]));
+          s = __fma_rn(q, q, s);
+        }
+      }
+      return exp(-s);
+    }
+    case FAM_C0: {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i)
+        if (i < d) s = __fma_rn(D.a[i], fabs(__dsub_rn(x[i], D.u[i])), s);
+      return exp(-s);
+    }
+    case FAM_DISCONTINUOUS: {
+      bool out = false;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i)
+        if (i < d) out = out || (x[i] > D.u[i]);
+      if (out) return 0.0;
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i)
+        if (i < d) s = __fma_rn(D.a[i], x[i], s);
+      return exp(s);
+    }
+    case FAM_PRODUCT: {
+      double v = x[0];
+#pragma unroll
+      for (int i = 1; i < MAXD; ++i)
+        if (i < d) v = __dmul_rn(v, x[i]);
+      return v;
+    }
+    case FAM_NAN:
+      return __longlong_as_double(0x7ff8000000000000LL);
+    case FAM_BOX: {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i)
+        if (i < d) s = __fma_rn(x[i], x[i], s);
+      return pow(s, __dmul_rn(0.5, D.c));
+    }
+    case FAM_FUN6: {
+      if (MAXD < 6) return 0.0;
+      const double t = __dmul_rn(__dmul_rn(pow(x[2], x[4]), x[3]), x[4]);
+      const double q = __dadd_rn(__dadd_rn(__dmul_rn(x[0], x[1]), __ddiv_rn(t, __dadd_rn(1.0, x[0]))),
+                                 __dmul_rn(x[5], x[5]));
+      return __dmul_rn(D.c, q);
+    }
+  }
+  return 0.0;
+}
+
+// Functor adapter used by the kernels for the C ABI families.
+struct FamilyFn {
+  template <int MAXD>
+  __device__ __forceinline__ double eval(const IntegralDesc& D, const double* x) const {
+    return family_eval<MAXD>(D, x);
+  }
+};
+
+}  // namespace pg

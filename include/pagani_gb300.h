@@ -1,0 +1,233 @@
+/*
+ * pagani_gb300.h -- C ABI of the GB300-native PAGANI / m-Cubes library.
+ *
+ * Plain C types only: pointers, sizes, PODs.  One pg_context owns its device
+ * memory (region pool, scratch, pinned host mirrors) and its CUDA stream; calls
+ * on one context are serialised, different contexts are independent.  No call
+ * aborts the process: every entry point returns a pg_status code, and
+ * pg_last_error() gives the message of the last failure on a context.
+ *
+ * Reference interfaces each entry point replaces are cited by file:line of the
+ * reference project (marcpaterno/gpuintegration).
+ */
+#ifndef PAGANI_GB300_H
+#define PAGANI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_MAX_DIM 16
+#define PG_MIN_NDIM 2
+#define PG_MAX_NDIM 10
+
+/* Return codes.  PG_NOT_CONVERGED mirrors the reference's status 1
+ * (common/integration_result.hh:17); the negative codes replace the
+ * reference's abort() on CUDA errors (common/cuda/cudaDebugUtil.h:119-151) and
+ * std::bad_alloc (common/cuda/cudaMemoryUtil.h:198-208). */
+typedef enum pg_status {
+  PG_OK = 0,
+  PG_NOT_CONVERGED = 1,
+  PG_BAD_ARG = -1,
+  PG_OOM = -2,
+  PG_CUDA_ERROR = -3,
+  PG_TIMEOUT = -4,
+  PG_UNSUPPORTED = -5,
+  PG_CANCELLED = -6
+} pg_status;
+
+/* Integrand families.  Device functors cannot cross a C ABI, so an integrand
+ * is named by family + parameters (the reference passes a functor:
+ * cuda/pagani/quad/GPUquad/Workspace.cuh:52-61).  The six Genz families follow
+ * common/cuda/integrands.cuh:1303-1934 with per-axis a_i (sharpness) and u_i
+ * (offset):
+ *   OSCILLATORY     cos(2*pi*u_0 + sum a_i x_i)
+ *   PRODUCT_PEAK    prod 1 / (a_i^-2 + (x_i - u_i)^2)
+ *   CORNER_PEAK     (1 + sum a_i x_i)^-(d+1)
+ *   GAUSSIAN        exp(-sum a_i^2 (x_i - u_i)^2)
+ *   C0              exp(-sum a_i |x_i - u_i|)
+ *   DISCONTINUOUS   0 if any x_i > u_i, else exp(sum a_i x_i)
+ * and the test integrands of the reference's own tests:
+ *   CONSTANT        c                                  (test/cuda/pagani/RegionSampling.cu:19-44)
+ *   PRODUCT         prod x_i                           (test/cuda/pagani/do_integration_from_c.cu:7-14)
+ *   NAN_VALUE       NaN                                (test/cuda/pagani/NanIntegral.cu:9-16)
+ *   BOX             (sum x_i^2)^(c/2)                  (cuda/pagani/demos/function.cuh:113-172)
+ *   FUN6            6-D test function of test/cuda/pagani/accuracy_improves_with_epsrel.cu:17-27 */
+typedef enum pg_family {
+  PG_FAMILY_CONSTANT = 0,
+  PG_FAMILY_OSCILLATORY = 1,
+  PG_FAMILY_PRODUCT_PEAK = 2,
+  PG_FAMILY_CORNER_PEAK = 3,
+  PG_FAMILY_GAUSSIAN = 4,
+  PG_FAMILY_C0 = 5,
+  PG_FAMILY_DISCONTINUOUS = 6,
+  PG_FAMILY_PRODUCT = 7,
+  PG_FAMILY_NAN_VALUE = 8,
+  PG_FAMILY_BOX = 9,
+  PG_FAMILY_FUN6 = 10,
+  PG_FAMILY_COUNT = 11
+} pg_family;
+
+typedef struct pg_integrand {
+  int32_t family; /* pg_family */
+  int32_t ndim;   /* 2..PG_MAX_NDIM */
+  double a[PG_MAX_DIM];
+  double u[PG_MAX_DIM];
+  double c;
+} pg_integrand;
+
+/* numint::integration_result (common/integration_result.hh:11-21).  neval is
+ * filled here (regions evaluated x points per region); the reference leaves it 0. */
+typedef struct pg_result {
+  double estimate;
+  double errorest;
+  double chi_sq;
+  uint64_t neval;
+  uint64_t nregions;
+  uint64_t nfinished;
+  uint64_t iters;
+  int32_t status;     /* 0 converged, 1 not converged (reference semantics) */
+  int32_t last_phase; /* -1 as in the reference */
+} pg_result;
+
+/* Options of the PAGANI iteration.  pg_options_default() gives the reference's
+ * behaviour: relative-error classification on (Workspace.cuh:360-368), 700
+ * iterations (Workspace.cuh:399), and the heuristic classifier's device-memory
+ * model fixed at 16e9 bytes (heuristic_classifier.cuh:89-94). */
+typedef struct pg_options {
+  int32_t relerr_classification;
+  int32_t max_iters;
+  double device_mem_model;  /* bytes seen by the memory-pressure classifier */
+  uint64_t max_regions;     /* hard cap of the region pool (0 = derived from the model) */
+  int32_t eval_mode;        /* 0 = exact reference order; see pg_eval_mode */
+  int32_t reserved;
+} pg_options;
+
+typedef enum pg_eval_mode {
+  PG_EVAL_REFERENCE_ORDER = 0, /* per-region sums in the reference's exact order */
+  PG_EVAL_FACTORED = 1         /* separable families: per-axis factors computed once per region */
+} pg_eval_mode;
+
+typedef struct pg_context pg_context;
+
+/* Kernel-level counters of a context (CUDA-event timed when profiling is on). */
+typedef struct pg_stats {
+  uint64_t launches;         /* kernels launched by this context */
+  uint64_t eval_launches;    /* region-evaluation launches */
+  uint64_t regions_evaluated;
+  uint64_t points_evaluated;
+  double eval_ms;            /* summed CUDA-event time of evaluation launches */
+  double stage_ms;           /* summed time of the two-level/classify/compact/split launches */
+  uint64_t stage_bytes;      /* algorithmic bytes moved by those stages */
+  uint64_t h2d_bytes;
+  uint64_t d2h_bytes;
+} pg_stats;
+
+void pg_options_default(pg_options* opt);
+int pg_feval(int ndim); /* points per region: cuda/pagani/quad/quad.h:67-76 */
+
+/* Context lifetime.  Replaces the reference's per-call allocations
+ * (Region_estimates.cuh:11-16, Sub_regions.cuh:199-207) with one pool. */
+int pg_context_create(int device, pg_context** out);
+int pg_context_destroy(pg_context* ctx);
+const char* pg_last_error(const pg_context* ctx);
+int pg_context_set_profiling(pg_context* ctx, int on);
+int pg_context_stats(const pg_context* ctx, pg_stats* out);
+int pg_context_reset_stats(pg_context* ctx);
+void* pg_context_stream(pg_context* ctx); /* the cudaStream_t the context launches on */
+int pg_synchronize(pg_context* ctx);
+
+/* Full PAGANI integration of one integrand over [lows, highs].
+ * Replaces Workspace<T,ndim>::integrate(f, epsrel, epsabs, vol, relerr)
+ * (cuda/pagani/quad/GPUquad/Workspace.cuh:361-494).  Returns the result status
+ * (PG_OK / PG_NOT_CONVERGED) or a negative error code.  lows/highs may be NULL
+ * for the unit cube. */
+int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double epsabs, const double* lows,
+                 const double* highs, const pg_options* opt, pg_result* out);
+
+/* Region evaluation on a caller-given region list (host buffers, SoA
+ * [dim * n + i]).  Replaces Cubature_rules::apply_cubature_integration_rules
+ * (cuda/pagani/quad/GPUquad/PaganiUtils.cuh:243-289), which the reference's
+ * stage tests call directly (test/cuda/pagani/RegionSampling.cu:48-88). */
+int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,
+                        uint64_t n, const double* left, const double* length, double* est, double* err,
+                        int32_t* bisect, int32_t eval_mode);
+
+/* Same on device buffers, asynchronous on the context stream. */
+int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,
+                               uint64_t n, const double* d_left, const double* d_length, double* d_est,
+                               double* d_err, int32_t* d_bisect, int32_t eval_mode);
+
+/* Two-level error estimate and relative-error classification on host buffers.
+ * Replaces two_level_errorest_and_relerr_classify / RefineError
+ * (cuda/pagani/quad/GPUquad/hybrid.cuh:11-45, Phases.cuh:219-268). */
+int pg_two_level(pg_context* ctx, uint64_t n, const double* est, const double* err, const double* parent_est,
+                 double* new_err, uint8_t* active, double epsrel, int32_t relerr_classification);
+
+/* Filter + split on host buffers: keeps the active regions in order and bisects
+ * each along its split axis; child 0 of the k-th kept region lands at k, child
+ * 1 at A + k, SoA stride 2A.  Replaces Sub_regions_filter::filter and
+ * Sub_region_splitter::split (Sub_region_filter.cuh:84-139,
+ * Sub_region_splitter.cuh:55-87).  *n_active receives A; out_left/out_length
+ * must hold 2*A*ndim doubles (A <= n). */
+int pg_filter_split(pg_context* ctx, int ndim, uint64_t n, const double* left, const double* length,
+                    const uint8_t* active, const int32_t* bisect, const double* est, const double* err,
+                    double* out_left, double* out_length, double* parent_est, double* parent_err,
+                    uint64_t* n_active);
+
+/* Deterministic compensated sum of n doubles on the GPU (blocked Neumaier
+ * order; see the library's reduction kernels).  Replaces reduction()
+ * (common/cuda/thrust_utils.cuh:37-47). */
+int pg_reduce_sum(pg_context* ctx, const double* x, uint64_t n, double* out);
+
+/* Exclusive scan of 0/1 flags, as used for compaction offsets.  Replaces
+ * exclusive_scan (common/cuda/thrust_utils.cuh:49-60). */
+int pg_exclusive_scan_flags(pg_context* ctx, const uint8_t* flags, uint64_t n, uint64_t* out, uint64_t* total);
+
+/* Degree-9 rule tables as generated by the library (host-side).  w, scale,
+ * norm: 45 doubles each ([set*5 + rule]); set_of: feval ints; gen: feval*ndim
+ * doubles, point-major.  Returns feval.  Mirrors quad::Rule<T>::Init
+ * (cuda/pagani/quad/GPUquad/Rule.cuh:370-510). */
+int pg_rule_tables(int ndim, double* w, double* scale, double* norm, int32_t* set_of, double* gen);
+
+/* The reference's C-language precedent, with the same contract:
+ * integrates x*y over the unit square at epsrel 1e-6, returns the status and
+ * writes the estimate only when it is 0.  test/cuda/pagani/do_integration_from_c.cu:21-37 */
+int do_integration_from_c(double* res);
+
+/* ---------------- m-Cubes (stratified VEGAS) ----------------
+ * Replaces cuda_mcubes::integrate<F,ndim>(f, epsrel, epsabs, ncall, &vol,
+ * totalIters, adjustIters, skipIters) (cuda/mcubes/vegasT.cuh:999-1030).
+ * The reference seeds from the wall clock (vegasT.cuh:801-803); here the
+ * Philox4x32-10 stream is keyed by `seed`, so runs are reproducible. */
+typedef struct pg_mcubes_options {
+  double ncall;      /* requested calls per iteration */
+  int32_t titer;     /* total iterations */
+  int32_t itmax;     /* adapting iterations */
+  int32_t skip;      /* iterations excluded from the weighted mean */
+  int32_t nbins;     /* bins per axis, 500 in the reference (vegasT.cuh:650) */
+  uint64_t seed;
+  double alpha;      /* grid damping exponent, 1.5 in the reference's GPU code */
+} pg_mcubes_options;
+
+void pg_mcubes_options_default(pg_mcubes_options* opt);
+int pg_mcubes_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double epsabs, const double* lows,
+                        const double* highs, const pg_mcubes_options* opt, pg_result* out);
+
+/* ---------------- batched PAGANI ----------------
+ * Integrates `count` independent integrands (any mix of ndim, family and
+ * tolerance) together: one device-side region pool shared by all of them, one
+ * evaluation launch per iteration over every live region of every integrand.
+ * No counterpart in the reference beyond running Workspace::integrate once per
+ * integrand (Workspace.cuh:361-494).  out[i] has the same semantics as
+ * pg_integrate's result for integrand i. */
+int pg_batch_integrate(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
+                       const double* epsabs, const pg_options* opt, pg_result* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PAGANI_GB300_H */

@@ -1,0 +1,949 @@
+// PAGANI CPU oracle -- TEST INFRASTRUCTURE ONLY.
+//
+// This file is the checker for the GB300 library: a plain C++ restatement of the
+// reference's PAGANI adaptive-cubature iteration.  Only tests/, the smoke check
+// and bench.py's CPU-baseline leg may load it.  The product path never calls it.
+//
+// Every stage cites the reference file:line it restates (paths relative to the
+// reference project root).  Floating-point contraction is written out explicitly
+// with std::fma at the places where nvcc contracts the reference's expressions;
+// the file is compiled with -ffp-contract=off so that nothing else is fused and
+// the results are the same on x86-64 and aarch64 hosts.
+//
+// Global reductions follow the library's deterministic blocked Neumaier order
+// (see canon_* below).  The reference uses thrust::reduce, whose order is
+// unspecified, so any fixed order is a faithful restatement; using the same
+// order as the GPU library makes GPU-vs-oracle comparisons bit-exact for
+// integrands that use only IEEE-exact operations.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+constexpr int kNRules = 5;  // cuda/pagani/quad/quad.h:65
+constexpr int kNSets = 9;   // cuda/pagani/quad/GPUquad/Rule.cuh:404-405
+constexpr int kMaxDim = 16;
+
+// ---------------------------------------------------------------------------
+// Integrand families (same struct layout as pg_integrand in the C ABI).
+// ---------------------------------------------------------------------------
+enum Family : int32_t {
+  FAM_CONSTANT = 0,
+  FAM_OSCILLATORY = 1,
+  FAM_PRODUCT_PEAK = 2,
+  FAM_CORNER_PEAK = 3,
+  FAM_GAUSSIAN = 4,
+  FAM_C0 = 5,
+  FAM_DISCONTINUOUS = 6,
+  FAM_PRODUCT = 7,
+  FAM_NAN = 8,
+  FAM_BOX = 9,
+  FAM_FUN6 = 10,
+};
+
+struct Integrand {
+  int32_t family;
+  int32_t ndim;
+  double a[kMaxDim];
+  double u[kMaxDim];
+  double c;
+};
+
+// Parameters derived once on the host.  The GPU library derives the same values
+// with the same operations (pg_prepare_integrand in the library).
+struct Prepared {
+  int family, ndim;
+  double a[kMaxDim], u[kMaxDim], ia2[kMaxDim];
+  double c, s0;
+};
+
+static Prepared prepare(const Integrand& f) {
+  Prepared p{};
+  p.family = f.family;
+  p.ndim = f.ndim;
+  for (int i = 0; i < kMaxDim; ++i) {
+    p.a[i] = f.a[i];
+    p.u[i] = f.u[i];
+    p.ia2[i] = 1.0 / (f.a[i] * f.a[i]);
+  }
+  p.c = f.c;
+  p.s0 = 2.0 * 3.14159265358979323846 * f.u[0];
+  if (f.family == FAM_FUN6)
+    p.c = 12.0 / (7.0 - 6.0 * std::log(2.0) * std::log(2.0) + std::log(64.0));
+  return p;
+}
+
+static inline double ipow(double s, int e) {
+  // Binary exponentiation with a fixed multiplication order.
+  double r = 1.0, b = s;
+  while (e) {
+    if (e & 1) r = r * b;
+    e >>= 1;
+    if (e) b = b * b;
+  }
+  return r;
+}
+
+static double eval(const Prepared& p, const double* x) {
+  const int d = p.ndim;
+  switch (p.family) {
+    case FAM_CONSTANT:
+      return p.c;
+    case FAM_OSCILLATORY: {
+      double s = p.s0;
+      for (int i = 0; i < d; ++i) s = std::fma(p.a[i], x[i], s);
+      return std::cos(s);
+    }
+    case FAM_PRODUCT_PEAK: {
+      double v = 1.0;
+      for (int i = 0; i < d; ++i) {
+        const double t = x[i] - p.u[i];
+        const double term = 1.0 / std::fma(t, t, p.ia2[i]);
+        v = (i == 0) ? term : v * term;
+      }
+      return v;
+    }
+    case FAM_CORNER_PEAK: {
+      double s = 1.0;
+      for (int i = 0; i < d; ++i) s = std::fma(p.a[i], x[i], s);
+      return 1.0 / ipow(s, d + 1);
+    }
+    case FAM_GAUSSIAN: {
+      double s = 0.0;
+      for (int i = 0; i < d; ++i) {
+        const double q = p.a[i] * (x[i] - p.u[i]);
+        s = std::fma(q, q, s);
+      }
+      return std::exp(-s);
+    }
+    case FAM_C0: {
+      double s = 0.0;
+      for (int i = 0; i < d; ++i) s = std::fma(p.a[i], std::fabs(x[i] - p.u[i]), s);
+      return std::exp(-s);
+    }
+    case FAM_DISCONTINUOUS: {
+      for (int i = 0; i < d; ++i)
+        if (x[i] > p.u[i]) return 0.0;
+      double s = 0.0;
+      for (int i = 0; i < d; ++i) s = std::fma(p.a[i], x[i], s);
+      return std::exp(s);
+    }
+    case FAM_PRODUCT: {
+      double v = x[0];
+      for (int i = 1; i < d; ++i) v = v * x[i];
+      return v;
+    }
+    case FAM_NAN:
+      return std::numeric_limits<double>::quiet_NaN();
+    case FAM_BOX: {
+      double s = 0.0;
+      for (int i = 0; i < d; ++i) s = std::fma(x[i], x[i], s);
+      return std::pow(s, 0.5 * p.c);
+    }
+    case FAM_FUN6: {
+      // test/cuda/pagani/accuracy_improves_with_epsrel.cu:267-275
+      const double t = (std::pow(x[2], x[4]) * x[3]) * x[4];
+      return p.c * ((x[0] * x[1] + t / (1.0 + x[0])) + x[5] * x[5]);
+    }
+  }
+  return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Degree-9 cubature rule tables.
+// Restates cuda/pagani/quad/GPUquad/Rule.cuh:24-270 (weights, generators,
+// null-rule scale/norm) and :409-507 (point enumeration order).  The weight
+// polynomials in NDIM are evaluated with the same grouping as the reference so
+// that every table entry is the same double.
+// ---------------------------------------------------------------------------
+struct Rule {
+  int ndim = 0, feval = 0;
+  double w[kNSets * kNRules];
+  double scale[kNSets * kNRules];
+  double norm[kNSets * kNRules];
+  double G[5];
+  std::vector<int> set_of;     // [feval]
+  std::vector<double> gen;     // [feval * ndim], point-major
+};
+
+int feval_count(int d) {
+  // cuda/pagani/quad/quad.h:67-76
+  return 1 + 8 * d + 2 * d * (d - 1) + 4 * d * (d - 1) + 4 * d * (d - 1) * (d - 2) / 3 + (1 << d);
+}
+
+static void rule9_weights(int ndim, double* w) {
+  const double n = (double)ndim;
+  // Constants of the degree-9 rule (Rule.cuh:36-147).
+  const double c1 = -.002361170967785511788400941242259231309691;
+  const double c2 = .1141539002385732526821323741697655347686;
+  const double c3 = -.6383392007670238909386026193674701393074;
+  const double c4 = .7484998850468520800423030047583803945205;
+  const double d1 = -.001432401703339912514196154599769007103671;
+  const double d2 = .05747150786448972594860897296200006759892;
+  const double d3 = -.1422510457143424323449521620935950679394;
+  const double d4 = -.06287502873828697998942424881040490136987;
+  const double e1 = .2545911332489590890011611142429070613156;
+  const double f1 = -1.207328566678236261002219995185143356737;
+  const double f2 = .8956736576416067650809467826488567200939;
+  const double g1 = -.3647935698604914666100134551377381205297;
+  const double h1 = .003541756451678267682601411863388846964536;
+  const double h2 = -.07260936739589367960492815865074633743652;
+  const double h3 = .1055749162521899101218622863269817454540;
+  const double i1 = .002148602555009868771294231899653510655506;
+  const double i2 = -.03226856389295394999786630399875134318006;
+  const double i3 = .01063678399023121748083624225818915724455;
+  const double j1 = .01468910249614349017540783437728097691502;
+  const double k1 = .5113470834646759143109387357149329909126;
+  const double k2 = .4597644812080634464633352781605214342691;
+  const double l1 = .1823967849302457333050067275688690602649;
+  const double m1 = -.04508628929435784075980562738240804429658;
+  const double m2 = .2141588352435279340097929526588394300172;
+  const double n1 = -.02735154652654564472203690086290223507436;
+  const double n2 = .05494106704871123410060080562462135546101;
+  const double o1 = .1193759620257077529708962121565290178730;
+  const double p1 = .6508951939192025059314756320878023215278;
+  const double p2 = .1474493982943446016775696826942585013243;
+  const double q1 = .01553241727660705326386197156586357005224;
+  const double r1 = .003532809960709087023561817517751309380604;
+  const double s1 = .09231719987444221619017126187763868745587;
+  const double t1 = .2515001149531479199576969952416196054795;
+  const double pow2 = (double)(1 << ndim);
+
+  const double pc = n * (n * (n * c1 + c2) + c3) + c4;  // shared cubic
+  const double pd = n * (n * (n * d1 + d2) + d3) - d4;
+  const double ph = n * (n * h1 + h2) + h3;
+  const double pi = n * (n * i1 + i2) + i3;
+  const double pm = n * m1 + m2;
+  const double pn = n * n1 + n2;
+
+  double tab[kNSets * kNRules] = {
+      // set 0: centre
+      pc, pd, n * e1 - pd, ((n * (n * f1 + f2) - 1) + n * (n * (n * c1 + c2) + c3)) + c4, (n * g1 + 1) - pc,
+      // set 1
+      ph, pi, j1 - pi, ((n * k1 + k2) + n * (n * h1 + h2)) + h3, l1 - ph,
+      // set 2
+      pm, pn, o1 - pn, n * p1 + p2, -pm,
+      // set 3
+      .05769338449097348357291272840392627722165, .03499962660214358382244159694487155861542,
+      -.05769338449097348357291272840392627722165, -1.386862771927828143599782668709014266770,
+      -.05769338449097348357291272840392627722165,
+      // set 4
+      0, 0, -.2386668732575008878964134721962088068396, 0, 0,
+      // set 5
+      q1 - n * h1, r1 - n * i1, -(r1 - n * i1), (s1 + q1) - n * h1, -(q1 - n * h1),
+      // set 6
+      .02254314464717892037990281369120402214829, .01367577326327282236101845043145111753718,
+      -.01367577326327282236101845043145111753718, -.3254475969596012529657378160439011607639,
+      -.02254314464717892037990281369120402214829,
+      // set 7
+      .001770878225839133841300705931694423482268, .001074301277504934385647115949826755327753,
+      -.001074301277504934385647115949826755327753, .001770878225839133841300705931694423482268,
+      -.001770878225839133841300705931694423482268,
+      // set 8
+      t1 / pow2, d4 / pow2, -(d4 / pow2), t1 / pow2, -(t1 / pow2)};
+  std::memcpy(w, tab, sizeof(tab));
+}
+
+static Rule make_rule(int ndim) {
+  Rule R;
+  R.ndim = ndim;
+  R.feval = feval_count(ndim);
+  rule9_weights(ndim, R.w);
+  R.G[0] = .4779536579022695061928604197171830064732;
+  R.G[1] = .2030285873691198677998034402373279133258;
+  R.G[2] = .4476273546261781288207704806530998539285;
+  R.G[3] = .125;
+  R.G[4] = .3430378987808781457001426145164678603407;
+  const int d = ndim;
+  const int count[kNSets] = {1,         2 * d, 2 * d, 2 * d, 2 * d, 2 * d * (d - 1), 4 * d * (d - 1),
+                             4 * d * (d - 1) * (d - 2) / 3, 1 << d};
+  // Null-rule scale and normalisation (Rule.cuh:256-269).
+  for (int i = 0; i < kNSets * kNRules; ++i) R.scale[i] = R.norm[i] = 0.0;
+  for (int idx = 0; idx < kNSets; ++idx) {
+    const double* sw = &R.w[idx * kNRules];
+    for (int r = 1; r < kNRules - 1; ++r) {
+      const double sc = (sw[r] == 0) ? 100 : -sw[r + 1] / sw[r];
+      double sum = 0;
+      for (int x = 0; x < kNSets; ++x) {
+        const double* wx = &R.w[x * kNRules];
+        sum += count[x] * std::fabs(wx[r + 1] + sc * wx[r]);
+      }
+      R.scale[idx * kNRules + r] = sc;
+      R.norm[idx * kNRules + r] = 1 / sum;
+    }
+  }
+  // Starting generator of each set (Rule.cuh:221-249).
+  std::vector<double> g0(kNSets * d, 0.0);
+  g0[d * 1] = R.G[0];
+  g0[d * 2] = R.G[1];
+  g0[d * 3] = R.G[2];
+  g0[d * 4] = R.G[3];
+  g0[d * 5] = R.G[0];
+  g0[d * 5 + 1] = R.G[0];
+  g0[d * 6] = R.G[0];
+  g0[d * 6 + 1] = R.G[1];
+  g0[d * 7] = R.G[0];
+  if (d >= 2) g0[d * 7 + 1] = R.G[0];
+  if (d >= 3) g0[d * 7 + 2] = R.G[0];
+  for (int k = 0; k < d; ++k) g0[d * 8 + k] = R.G[4];
+
+  // Enumerate the sign changes and permutations of every generator in the
+  // reference's order (Rule.cuh:438-504): signs advance like a binary counter
+  // from axis 0; when they wrap, the magnitudes step to the next permutation.
+  R.set_of.clear();
+  R.gen.clear();
+  for (int s = 0; s < kNSets; ++s) {
+    std::vector<double> g(g0.begin() + s * d, g0.begin() + (s + 1) * d);
+    for (int m = 0; m < count[s]; ++m) {
+      R.set_of.push_back(s);
+      for (int k = 0; k < d; ++k) R.gen.push_back(g[k] == 0.0 ? 0.0 : g[k]);
+      bool more_signs = false;
+      for (int k = 0; k < d; ++k) {
+        g[k] = -g[k];
+        if (g[k] < -0.0000000000000001) {
+          more_signs = true;
+          break;
+        }
+      }
+      if (more_signs) continue;
+      for (int k = 1; k < d; ++k) {
+        const double gk = g[k];
+        if (g[k - 1] > gk) {
+          size_t i, j = k, ix = k, dx = k - 1;
+          for (i = 0; i < --j; ++i) {
+            const double tmp = g[i];
+            g[i] = g[j];
+            g[j] = tmp;
+            if (tmp <= gk) --dx;
+            if (g[i] > gk) ix = i;
+          }
+          if (g[dx] <= gk) dx = ix;
+          g[k] = g[dx];
+          g[dx] = gk;
+          break;
+        }
+      }
+    }
+  }
+  return R;
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic blocked Neumaier reductions (the library's reduction order).
+// Chunk = 2048 elements, 256 lanes x 8 items per lane (stride 256), lane
+// partials merged by a shuffle-down tree per 32-lane warp, then the 8 warp
+// partials by a tree with offsets 4,2,1.  Chunk partials are merged by one
+// 256-lane pass (lane t takes chunks t, t+256, ...) and the same trees.
+// ---------------------------------------------------------------------------
+struct NS {
+  double s, c;
+};
+
+static inline NS ns_merge(NS a, NS b) {
+  const double t = a.s + b.s;
+  const double e = (std::fabs(a.s) >= std::fabs(b.s)) ? ((a.s - t) + b.s) : ((b.s - t) + a.s);
+  return NS{t, (a.c + b.c) + e};
+}
+
+static NS ns_block_tree(NS* lane) {
+  // lane[0..255]; warp trees then warp-0 tree.
+  NS warp[8];
+  for (int w = 0; w < 8; ++w) {
+    NS v[32];
+    for (int l = 0; l < 32; ++l) v[l] = lane[w * 32 + l];
+    for (int off = 16; off >= 1; off >>= 1)
+      for (int l = 0; l < off; ++l) v[l] = ns_merge(v[l], v[l + off]);
+    warp[w] = v[0];
+  }
+  for (int off = 4; off >= 1; off >>= 1)
+    for (int l = 0; l < off; ++l) warp[l] = ns_merge(warp[l], warp[l + off]);
+  return warp[0];
+}
+
+template <class Get>
+static double canon_sum(size_t n, Get get) {
+  const size_t nchunks = (n + 2047) / 2048;
+  std::vector<NS> part(nchunks);
+  for (size_t b = 0; b < nchunks; ++b) {
+    NS lane[256];
+    for (int t = 0; t < 256; ++t) {
+      NS acc{0.0, 0.0};
+      for (int k = 0; k < 8; ++k) {
+        const size_t i = b * 2048 + (size_t)k * 256 + t;
+        if (i < n) acc = ns_merge(acc, NS{get(i), 0.0});
+      }
+      lane[t] = acc;
+    }
+    part[b] = ns_block_tree(lane);
+  }
+  NS lane[256];
+  for (int t = 0; t < 256; ++t) {
+    NS acc{0.0, 0.0};
+    for (size_t b = t; b < nchunks; b += 256) acc = ns_merge(acc, part[b]);
+    lane[t] = acc;
+  }
+  const NS r = ns_block_tree(lane);
+  return r.s + r.c;
+}
+
+// ---------------------------------------------------------------------------
+// Region evaluation.  Restates INIT_REGION_POOL (Phases.cuh:301-363) and
+// SampleRegionBlock / computePermutation (Sample.cuh:103-290) for one region,
+// including the reduction order of the 64-thread block: thread t accumulates
+// points t, t+64, ... with a fused multiply-add, the two 32-lane warps reduce
+// with shuffle-down offsets 16..1 and the block sum is (warp0 + 0) + warp1
+// (Sample.cuh:49-83).
+// ---------------------------------------------------------------------------
+struct EvalOut {
+  double est, err;
+  int bisect;
+};
+
+static EvalOut eval_region(const Rule& R, const Prepared& P, const double* lows, const double* highs,
+                           const double* lower, const double* length) {
+  const int d = R.ndim;
+  double lo[kMaxDim], hi[kMaxDim], glo[kMaxDim], range[kMaxDim];
+  double jac = 1.0, vol = 1.0, maxRange = 0.0;
+  int maxDim = 0;
+  for (int k = 0; k < d; ++k) {
+    lo[k] = lower[k];
+    hi[k] = lo[k] + length[k];
+    vol *= hi[k] - lo[k];
+    glo[k] = lows[k];
+    range[k] = highs[k] - lows[k];
+    const double r = hi[k] - lo[k];
+    jac = jac * range[k];
+    if (r > maxRange) {
+      maxDim = k;
+      maxRange = r;
+    }
+  }
+  double lane_sum[64][kNRules];
+  std::memset(lane_sum, 0, sizeof(lane_sum));
+  double f64[64];
+  double x[kMaxDim];
+  for (int p = 0; p < R.feval; ++p) {
+    const double* g = &R.gen[(size_t)p * d];
+    for (int k = 0; k < d; ++k) {
+      const double A = .5 + g[k], B = .5 - g[k];
+      const double t = std::fma(A, lo[k], B * hi[k]);
+      x[k] = std::fma(t, range[k], glo[k]);
+    }
+    const double fun = eval(P, x) * jac;
+    if (p < 64) f64[p] = fun;
+    const double* w = &R.w[R.set_of[p] * kNRules];
+    double* acc = lane_sum[p & 63];
+    for (int r = 0; r < kNRules; ++r) acc[r] = std::fma(fun, w[r], acc[r]);
+  }
+  // Fourth differences and split axis (Sample.cuh:194-218).
+  int bisect = maxDim;
+  {
+    const double q = R.G[1] / R.G[0];
+    const double ratio = q * q;
+    const double base = (f64[0] * 2) * (1 - ratio);
+    double maxdiff = 0;
+    for (int k = 0; k < d; ++k) {
+      const double fp = f64[1 + 2 * k], fm = f64[2 + 2 * k];
+      const double fp2 = f64[1 + 2 * k + 2 * d], fm2 = f64[2 + 2 * k + 2 * d];
+      const double fd = std::fabs(std::fma(ratio, fp + fm, base) - (fp2 + fm2));
+      if (fd > maxdiff) {
+        maxdiff = fd;
+        bisect = k;
+      }
+    }
+  }
+  double sum[kNRules];
+  for (int r = 0; r < kNRules; ++r) {
+    double v[64];
+    for (int l = 0; l < 64; ++l) v[l] = lane_sum[l][r];
+    double warp_tot[2];
+    for (int w = 0; w < 2; ++w) {
+      double a[32];
+      for (int l = 0; l < 32; ++l) a[l] = v[w * 32 + l];
+      for (int off = 16; off >= 1; off >>= 1)
+        for (int l = 0; l < off; ++l) a[l] = a[l] + a[l + off];
+      warp_tot[w] = a[0];
+    }
+    sum[r] = (warp_tot[0] + 0.0) + warp_tot[1];
+  }
+  // Null-rule error (Sample.cuh:261-289).
+  for (int r = 1; r < kNRules - 1; ++r) {
+    double maxerr = 0.;
+    for (int s = 0; s < kNSets; ++s)
+      maxerr = std::fmax(maxerr, std::fabs(std::fma(R.scale[s * kNRules + r], sum[r], sum[r + 1])) *
+                                     R.norm[s * kNRules + r]);
+    sum[r] = maxerr;
+  }
+  EvalOut o;
+  o.est = vol * sum[0];
+  o.err = vol * ((5. * sum[1] <= sum[2] && 5. * sum[2] <= sum[3])
+                     ? 1. * sum[1]
+                     : 5. * std::fmax(std::fmax(sum[1], sum[2]), sum[3]));
+  o.bisect = bisect;
+  return o;
+}
+
+static void parallel_for(size_t n, int nthreads, const std::function<void(size_t, size_t)>& body) {
+  if (nthreads <= 1 || n < 64) {
+    body(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const size_t per = (n + nthreads - 1) / nthreads;
+  for (int t = 0; t < nthreads; ++t) {
+    const size_t b = t * per, e = std::min(n, b + per);
+    if (b >= e) break;
+    th.emplace_back([&, b, e] { body(b, e); });
+  }
+  for (auto& t : th) t.join();
+}
+
+static void evaluate_all(const Rule& R, const Prepared& P, const double* lows, const double* highs, size_t n,
+                         const double* left, const double* len, double* est, double* err, int32_t* bis,
+                         int nthreads) {
+  const int d = R.ndim;
+  parallel_for(n, nthreads, [&](size_t b, size_t e) {
+    double lo[kMaxDim], ln[kMaxDim];
+    for (size_t i = b; i < e; ++i) {
+      for (int k = 0; k < d; ++k) {
+        lo[k] = left[(size_t)k * n + i];
+        ln[k] = len[(size_t)k * n + i];
+      }
+      const EvalOut o = eval_region(R, P, lows, highs, lo, ln);
+      est[i] = o.est;
+      err[i] = o.err;
+      bis[i] = o.bisect;
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Two-level error and relative-error classification.
+// Restates RefineError (Phases.cuh:219-268) as launched by
+// two_level_errorest_and_relerr_classify (hybrid.cuh:11-45).
+// ---------------------------------------------------------------------------
+static void two_level(size_t n, const double* est, const double* err, const double* parent_est, double* new_err,
+                      uint8_t* active, double epsrel, bool relerr_classification) {
+  for (size_t tid = 0; tid < n; ++tid) {
+    double selfErr = err[tid];
+    const double selfRes = est[tid];
+    const size_t inRight = (2 * tid >= n);
+    const size_t sib = inRight ? tid - n / 2 : tid + n / 2;
+    const size_t par = tid - inRight * (n / 2);
+    const double siblErr = err[sib], siblRes = est[sib];
+    const double parRes = parent_est[par];
+    double diff = siblRes + selfRes - parRes;
+    diff = std::fabs(.25 * diff);
+    const double e2 = selfErr + siblErr;
+    if (e2 > 0.0) {
+      const double c = 1 + 2 * diff / e2;
+      selfErr *= c;
+    }
+    selfErr += diff;
+    new_err[tid] = selfErr;
+    const bool pass = relerr_classification && selfErr < std::fmax(epsrel * std::fabs(selfRes), 1e-200);
+    active[tid] = pass ? 0 : 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Heuristic memory-pressure classifier.
+// Restates cuda/pagani/quad/GPUquad/heuristic_classifier.cuh:89-452 and
+// Workspace::heuristic_classify (Workspace.cuh:74-118).  The device memory is
+// a parameter; the reference hard-codes 16e9 bytes (heuristic_classifier.cuh:89-94).
+// ---------------------------------------------------------------------------
+struct Classifier {
+  double epsrel = 0, epsabs = 0;
+  int required_digits = 0;
+  double last[3] = {0, 0, 0};  // uninitialised in the reference; zero here
+  size_t iters_collected = 0;
+  double max_percent_error_budget = .25;
+  double max_active_regions_percentage = .5;
+  int ndim = 0;
+  double total_mem = 16e9;
+
+  size_t mem_required(size_t n) const {
+    const size_t doubles = n + n + 2 * n + 2 * n + 2 * n * ndim + 2 * n * ndim + n * ndim * 2 + n * ndim * 2 + n +
+                           n + n * ndim + n * ndim;
+    const size_t ints = n + 2 * n + n;
+    return 8 * doubles + 4 * ints;
+  }
+  size_t free_mem(size_t n) const {
+    const size_t total = (size_t)total_mem;
+    const size_t occ = mem_required(n);
+    return total > occ ? total - occ : 1;
+  }
+  static std::string fixed15(double v) {
+    std::ostringstream out;
+    out.precision(15);
+    out << std::fixed << v;
+    return out.str();
+  }
+  bool sig_digits_same() const {
+    double third = std::fabs(last[0]), second = std::fabs(last[1]), first = std::fabs(last[2]);
+    while (first != 0. && first < 1.) first *= 10;
+    while (second != 0. && second < 1.) second *= 10;
+    while (third != 0. && third < 1.) third *= 10;
+    const std::string a = fixed15(third), b = fixed15(second), c = fixed15(first);
+    bool verdict = true;
+    int sig = 0;
+    for (int i = 0; i < required_digits + 1 && sig < required_digits && verdict; ++i) {
+      const char ci = i < (int)c.size() ? c[i] : '\0';
+      const char bi = i < (int)b.size() ? b[i] : '\0';
+      const char ai = i < (int)a.size() ? a[i] : '\0';
+      verdict = (ci == bi && bi == ai);
+      sig += (verdict && ci != '.') ? 1 : 0;
+    }
+    return verdict;
+  }
+  bool estimate_converged() const { return !(iters_collected - 1 < 1 || !sig_digits_same()); }
+  void store(double e) {
+    last[0] = last[1];
+    last[1] = last[2];
+    last[2] = e;
+    iters_collected++;
+  }
+  bool criteria_met(size_t n) const {
+    const double ratio = (double)mem_required(n) / (double)free_mem(n);
+    if (ratio > 1.) return true;
+    if (ratio > .1 && estimate_converged()) return true;
+    return false;
+  }
+};
+
+struct ClassRes {
+  bool pass_mem = false, pass_budget = false;
+  double threshold = 0, low = 0, high = 0;
+  size_t num_active = 0;
+  double finished_errorest = 0;
+  std::vector<uint8_t> flags;
+};
+
+static void apply_threshold(const Classifier& C, ClassRes& r, const double* err, size_t n) {
+  r.flags.resize(n);
+  for (size_t i = 0; i < n; ++i) r.flags[i] = err[i] > r.threshold ? 1 : 0;
+  r.num_active = (size_t)canon_sum(n, [&](size_t i) { return (double)r.flags[i]; });
+  const double pct = (double)(int)r.num_active / (double)(int)n;
+  r.pass_mem = pct <= C.max_active_regions_percentage;
+}
+
+static ClassRes classify(Classifier& C, const double* err, size_t n, double iter_err, double iter_fin_err,
+                         double total_fin_err) {
+  ClassRes r;
+  double mn = err[0], mx = err[0];
+  for (size_t i = 1; i < n; ++i) {
+    if (err[i] < mn) mn = err[i];
+    if (err[i] > mx) mx = err[i];
+  }
+  r.low = mn;
+  r.high = mx;
+  r.threshold = iter_err / n;
+  const double target = std::fabs(C.last[2]) * C.epsrel;
+  size_t inc = 0, dec = 0;
+  auto larger = [&]() {
+    r.pass_mem = false;
+    for (size_t cnt = 0; !r.pass_mem && cnt < 20; ++cnt) {
+      apply_threshold(C, r, err, n);
+      if (!r.pass_mem) {
+        r.low = r.threshold;
+        r.threshold += std::fabs(r.high - r.threshold) * .5;
+      }
+    }
+  };
+  do {
+    if (!r.pass_mem && inc <= 20) {
+      larger();
+      inc++;
+    }
+    if (r.pass_mem) {
+      const double dot = canon_sum(n, [&](size_t i) { return err[i] * (double)r.flags[i]; });
+      const double extra = iter_err - dot - iter_fin_err;
+      const double budget = target - total_fin_err;
+      r.pass_budget = extra <= C.max_percent_error_budget * budget;
+      r.finished_errorest = extra;
+      if (!r.pass_budget && dec <= 20) {
+        r.high = r.threshold;
+        r.threshold -= std::fabs(r.low - r.threshold) * .5;
+        r.pass_mem = false;
+        dec++;
+      }
+    }
+    const bool exhausted = dec >= 20 || inc >= 20;
+    if (exhausted && C.max_percent_error_budget < .7) {
+      C.max_percent_error_budget += 0.1;
+      dec = inc = 0;
+      r.low = mn;
+      r.high = mx;
+      r.threshold = iter_err / n;
+    } else if (exhausted && C.max_percent_error_budget >= .7 && C.max_active_regions_percentage <= .7) {
+      C.max_active_regions_percentage += .1;
+    } else if (exhausted) {
+      break;
+    }
+  } while (!r.pass_mem || !r.pass_budget);
+  C.max_active_regions_percentage = .5;
+  C.max_percent_error_budget = .25;
+  return r;
+}
+
+}  // namespace orc
+
+// ---------------------------------------------------------------------------
+// C interface used by the Python test harness.
+// ---------------------------------------------------------------------------
+extern "C" {
+
+typedef struct {
+  double estimate, errorest, chi_sq;
+  uint64_t neval, nregions, nfinished, iters;
+  int32_t status, last_phase;
+} orc_result;
+
+int orc_feval(int ndim) { return orc::feval_count(ndim); }
+
+// Rule tables: w/scale/norm [45], set_of [feval], gen [feval*ndim] (point-major).
+int orc_rule_tables(int ndim, double* w, double* scale, double* norm, int32_t* set_of, double* gen) {
+  if (ndim < 2 || ndim > 15) return -1;
+  const orc::Rule R = orc::make_rule(ndim);
+  std::memcpy(w, R.w, sizeof(R.w));
+  std::memcpy(scale, R.scale, sizeof(R.scale));
+  std::memcpy(norm, R.norm, sizeof(R.norm));
+  for (int p = 0; p < R.feval; ++p) set_of[p] = R.set_of[p];
+  std::memcpy(gen, R.gen.data(), sizeof(double) * R.gen.size());
+  return R.feval;
+}
+
+double orc_eval_point(const orc::Integrand* f, const double* x) {
+  const orc::Prepared P = orc::prepare(*f);
+  return orc::eval(P, x);
+}
+
+int orc_evaluate_regions(const orc::Integrand* f, const double* lows, const double* highs, uint64_t n,
+                         const double* left, const double* length, double* est, double* err, int32_t* bisect,
+                         int nthreads) {
+  const int d = f->ndim;
+  if (d < 2 || d > 15) return -1;
+  const orc::Rule R = orc::make_rule(d);
+  const orc::Prepared P = orc::prepare(*f);
+  orc::evaluate_all(R, P, lows, highs, n, left, length, est, err, bisect, nthreads);
+  return 0;
+}
+
+int orc_two_level(uint64_t n, const double* est, const double* err, const double* parent_est, double* new_err,
+                  uint8_t* active, double epsrel, int relerr_classification) {
+  orc::two_level(n, est, err, parent_est, new_err, active, epsrel, relerr_classification != 0);
+  return 0;
+}
+
+double orc_canon_sum(const double* x, uint64_t n) {
+  return orc::canon_sum(n, [&](size_t i) { return x[i]; });
+}
+
+// Uniform initial split (Sub_regions.cuh:11-36,253-274; partition rule Workspace.cuh:379-387).
+uint64_t orc_uniform_split(int ndim, int parts, double* left, double* length) {
+  size_t n = 1;
+  for (int k = 0; k < ndim; ++k) n *= parts;
+  if (!left) return n;
+  const double len = 1. / (double)parts;
+  for (size_t r = 0; r < n; ++r) {
+    size_t q = r;
+    for (int k = 0; k < ndim; ++k) {
+      const size_t id = q % parts;
+      q /= parts;
+      left[(size_t)k * n + r] = (double)id * len;
+      length[(size_t)k * n + r] = len;
+    }
+  }
+  return n;
+}
+
+// Filter (Sub_region_filter.cuh:8-139) + split (Sub_region_splitter.cuh:8-88):
+// compacts active regions in order and bisects each along its split axis.
+// Output holds 2*A regions: child 0 at k, child 1 at A+k.  Returns A.
+uint64_t orc_filter_split(int ndim, uint64_t n, const double* left, const double* length, const uint8_t* active,
+                          const int32_t* bisect, const double* est, const double* err, double* out_left,
+                          double* out_length, double* parent_est, double* parent_err) {
+  size_t A = 0;
+  for (size_t i = 0; i < n; ++i) A += active[i] ? 1 : 0;
+  size_t k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    if (!active[i]) continue;
+    if (parent_est) parent_est[k] = est[i];
+    if (parent_err) parent_err[k] = err[i];
+    const int bd = bisect[i];
+    for (int dd = 0; dd < ndim; ++dd) {
+      const double l = left[(size_t)dd * n + i], h = length[(size_t)dd * n + i];
+      if (dd == bd) {
+        const double half = h / 2;
+        out_left[(size_t)dd * 2 * A + k] = l + 0 * half;
+        out_left[(size_t)dd * 2 * A + A + k] = l + 1 * half;
+        out_length[(size_t)dd * 2 * A + k] = half;
+        out_length[(size_t)dd * 2 * A + A + k] = half;
+      } else {
+        out_left[(size_t)dd * 2 * A + k] = l;
+        out_left[(size_t)dd * 2 * A + A + k] = l;
+        out_length[(size_t)dd * 2 * A + k] = h;
+        out_length[(size_t)dd * 2 * A + A + k] = h;
+      }
+    }
+    ++k;
+  }
+  return A;
+}
+
+// Full PAGANI iteration: Workspace::integrate, self-splitting overload
+// (Workspace.cuh:361-494), with fix_error_budget_overflow (:121-146) and
+// heuristic_classify (:74-118).  trace (optional) receives, per iteration,
+// [N, A_after_classification, iter_est, iter_err, cumm_est, cumm_err].
+int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const double* lows, const double* highs,
+                  int relerr_classification, double total_device_mem, int max_iters, int nthreads, orc_result* out,
+                  double* trace, int trace_cap) {
+  using namespace orc;
+  const int d = f->ndim;
+  if (d < 2 || d > 15 || !out) return -1;
+  const Rule R = make_rule(d);
+  const Prepared P = prepare(*f);
+  const int parts = d < 5 ? 4 : (d <= 10 ? 2 : 1);
+  size_t n = orc_uniform_split(d, parts, nullptr, nullptr);
+  std::vector<double> left(n * d), len(n * d);
+  orc_uniform_split(d, parts, left.data(), len.data());
+  std::vector<double> parent_est, parent_err;
+  bool have_parent = false;
+  Classifier C;
+  C.epsrel = epsrel;
+  C.epsabs = epsabs;
+  C.required_digits = (int)std::ceil(std::log10(1 / epsrel));
+  C.ndim = d;
+  C.total_mem = total_device_mem > 0 ? total_device_mem : 16e9;
+  orc_result cum{};
+  cum.status = 1;
+  cum.last_phase = -1;
+  const uint64_t fev = (uint64_t)R.feval;
+  std::vector<double> est, err, nerr;
+  std::vector<int32_t> bis;
+  std::vector<uint8_t> act;
+  int ntrace = 0;
+  for (int it = 0; it < max_iters && n > 0; ++it) {
+    est.assign(n, 0);
+    err.assign(n, 0);
+    bis.assign(n, 0);
+    act.assign(n, 1);
+    evaluate_all(R, P, lows, highs, n, left.data(), len.data(), est.data(), err.data(), bis.data(), nthreads);
+    cum.neval += n * fev;
+    const double iter_est = canon_sum(n, [&](size_t i) { return est[i]; });
+    if (have_parent) {
+      nerr.assign(n, 0);
+      two_level(n, est.data(), err.data(), parent_est.data(), nerr.data(), act.data(), epsrel,
+                relerr_classification != 0);
+      err.swap(nerr);
+    }
+    const double iter_err = canon_sum(n, [&](size_t i) { return err[i]; });
+    double* tr = (trace && ntrace < trace_cap) ? trace + 6 * ntrace : nullptr;
+    if (tr) {
+      tr[0] = (double)n;
+      tr[2] = iter_est;
+      tr[3] = iter_err;
+      ++ntrace;
+    }
+    const double cest = std::fabs(cum.estimate + iter_est), cerr = cum.errorest + iter_err;
+    if (cerr / cest <= epsrel || cerr <= epsabs) {
+      cum.estimate += iter_est;
+      cum.errorest += iter_err;
+      cum.status = 0;
+      cum.nregions += n;
+      if (tr) {
+        tr[1] = 0;
+        tr[4] = cum.estimate;
+        tr[5] = cum.errorest;
+      }
+      *out = cum;
+      return ntrace;
+    }
+    C.store(cum.estimate + iter_est);
+    double fin_est = iter_est - canon_sum(n, [&](size_t i) { return (double)act[i] * est[i]; });
+    double fin_err = iter_err - canon_sum(n, [&](size_t i) { return (double)act[i] * err[i]; });
+    // fix_error_budget_overflow
+    {
+      const double leaves_est = cum.estimate + iter_est;
+      const double leaves_fin_err = cum.errorest + fin_err;
+      if (leaves_fin_err > std::fabs(leaves_est) * epsrel) {
+        std::fill(act.begin(), act.end(), 1);
+        fin_err = 0.;
+        fin_est = 0.;
+      }
+    }
+    // heuristic_classify
+    bool must_terminate;
+    {
+      const double ratio = (double)C.mem_required(n) / (double)C.free_mem(n);
+      const bool necessary = ratio > 1.;
+      if (!C.criteria_met(n)) {
+        must_terminate = necessary;
+      } else {
+        ClassRes hs = classify(C, err.data(), n, iter_err, fin_err, cum.errorest);
+        const bool ok = hs.pass_mem && hs.pass_budget;
+        if (ok) {
+          act = hs.flags;
+          fin_est = iter_est - canon_sum(n, [&](size_t i) { return (double)act[i] * est[i]; });
+          fin_err = hs.finished_errorest;
+        }
+        must_terminate = (!ok && necessary) || hs.num_active == 0;
+      }
+    }
+    if (must_terminate) {
+      cum.estimate += iter_est;
+      cum.errorest += iter_err;
+      cum.nregions += n;
+      if (tr) {
+        tr[1] = -1;
+        tr[4] = cum.estimate;
+        tr[5] = cum.errorest;
+      }
+      *out = cum;
+      return ntrace;
+    }
+    cum.estimate += fin_est;
+    cum.errorest += fin_err;
+    // filter
+    size_t A = 0;
+    for (size_t i = 0; i < n; ++i) A += act[i];
+    if (tr) {
+      tr[1] = (double)A;
+      tr[4] = cum.estimate;
+      tr[5] = cum.errorest;
+    }
+    cum.nregions += n - A;
+    cum.nfinished += n - A;
+    if (A == 0) {
+      n = 0;
+      cum.iters++;
+      break;
+    }
+    std::vector<double> nl(2 * A * d), nln(2 * A * d);
+    parent_est.assign(A, 0);
+    parent_err.assign(A, 0);
+    orc_filter_split(d, n, left.data(), len.data(), act.data(), bis.data(), est.data(), err.data(), nl.data(),
+                     nln.data(), parent_est.data(), parent_err.data());
+    have_parent = true;
+    left.swap(nl);
+    len.swap(nln);
+    n = 2 * A;
+    cum.iters++;
+  }
+  cum.nregions += n;
+  *out = cum;
+  return ntrace;
+}
+
+}  // extern "C"

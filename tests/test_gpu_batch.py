@@ -1,0 +1,33 @@
+"""Batched PAGANI: each integral's result is identical alone and in a batch."""
+import numpy as np
+import pytest
+
+import gpuintegration_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed(rng, count):
+    fams = list(pg.GENZ_FAMILIES)
+    sums = {pg.OSCILLATORY: 6.0, pg.PRODUCT_PEAK: 9.0, pg.CORNER_PEAK: 7.0, pg.GAUSSIAN: 26.0, pg.C0: 12.0,
+            pg.DISCONTINUOUS: 6.3}
+    out = []
+    for _ in range(count):
+        d = int(rng.integers(2, 9))
+        fam = fams[int(rng.integers(0, 6))]
+        a = rng.random(d)
+        a *= sums[fam] / a.sum()
+        u = rng.random(d)
+        out.append(pg.genz(fam, a, u))
+    return out
+
+
+def test_batch_equals_individual_runs(ctx):
+    rng = np.random.default_rng(42)
+    fs = _mixed(rng, 24)
+    eps = 10 ** rng.uniform(-5, -3, size=len(fs))
+    batch = ctx.batch_integrate(fs, eps, 0.0)
+    for f, e, b in zip(fs, eps, batch):
+        r = ctx.integrate(f, float(e), 0.0)
+        assert (r.estimate, r.errorest, r.nregions, r.status, r.iters, r.neval) == \
+               (b.estimate, b.errorest, b.nregions, b.status, b.iters, b.neval)
