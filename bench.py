@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 PAGANI library on the batched Genz workload.
+
+Workload (one step): the 4096 pre-screened mixed Genz integrals of the
+batched configuration -- dim ~ U{2..8}, family ~ U{6 Genz families}, seeded
+a_i/u_i scaled per family, epsrel log-uniform in [1e-7, 1e-4], FP64, unit
+cube -- integrated together by pg_batch_integrate (one device region pool,
+one evaluation launch per iteration over every live region).
+
+Metric: converged integrals per second, where an integral counts when PAGANI
+reports status 0 and the estimate lies within its epsrel of the analytic
+value.  `value` is timed with CUDA events on the library's stream (the step's
+integrand descriptors are a few MB; everything else is produced on the
+device); `e2e` is the same metric by host wall clock around the C-ABI call,
+including the host->device copy of the descriptors and the device->host copy
+of the results.  p50/p99 are the per-integral completion latencies inside a
+step.  The reference arm (--impl reference) times the CPU restatement of
+PAGANI on all host cores on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "integrals/s at rel err <=1e-6, batched vs plain PAGANI on 1 GB300; p50/p99 latency"
+WORKLOAD = "batched PAGANI: 4096 pre-screened mixed Genz integrals, dim 2..8, 6 families, epsrel log-U[1e-7,1e-4]"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--count", type=int, default=4096)
+    p.add_argument("--plain-sample", type=int, default=512)
+    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--max-regions", type=int, default=1 << 26)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def flops_per_point(family, d):
+    import gpuintegration_gb300 as pg
+    if family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT):
+        f = d - 1  # product of the per-axis factors
+    elif family == pg.OSCILLATORY:
+        f = 2 * d + 1
+    elif family == pg.CORNER_PEAK:
+        e, muls, sq = d + 1, 0, 0
+        while e:
+            if e & 1:
+                muls += 1
+            e >>= 1
+            if e:
+                sq += 1
+        f = 2 * d + muls + sq + 1
+    else:
+        f = 2 * d + 1
+    return f + 10  # five rule sums (FMA = 2 flops)
+
+
+def flops_per_region(family, d):
+    import gpuintegration_gb300 as pg
+    factor = {pg.PRODUCT_PEAK: 4, pg.GAUSSIAN: 4, pg.C0: 3, pg.DISCONTINUOUS: 2, pg.PRODUCT: 0}.get(family, 0)
+    return 11 * d * (3 + factor) + 60 + (6 * d + 3) + 114 + 2 * d
+
+
+def algorithmic_flops(cases, results):
+    import gpuintegration_gb300 as pg
+    lib = pg.load_library()
+    tot = 0.0
+    for c, r in zip(cases, results):
+        f = c.integrand
+        fe = lib.pg_feval(f.ndim)
+        regions = r.neval // fe
+        tot += r.neval * flops_per_point(f.family, f.ndim) + regions * flops_per_region(f.family, f.ndim)
+    return tot
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def within(c, r):
+    from gpuintegration_gb300 import workloads as W
+    return r.status == 0 and W.within_tolerance(r.estimate, c.exact, c.epsrel)
+
+
+# ---------------------------------------------------------------------------
+CPU_SAMPLE_MAX_REGIONS = 200000
+
+
+def cpu_leg(cases, seconds, totals=None):
+    """Times the CPU oracle (all host threads) on the integrals of the workload,
+    in workload order, whose screened region count is at most
+    CPU_SAMPLE_MAX_REGIONS (so no single integral runs for minutes), until
+    `seconds` have passed; returns evaluation points/s and the sample."""
+    from oracle import oracle
+    oracle.load()
+    screen = json.load(open(os.path.join(ROOT, "tests", "golden", "config4_screen.json")))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    pts, done, conv = 0, 0, 0
+    for c, nreg in zip(cases, screen["nregions"]):
+        if nreg > CPU_SAMPLE_MAX_REGIONS:
+            continue
+        r, _ = oracle.integrate(c.integrand, c.epsrel, 0.0, nthreads=threads)
+        pts += r.neval
+        done += 1
+        conv += 1 if within(c, r) else 0
+        if time.perf_counter() - t0 >= seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"points_per_s": pts / el, "integrals": done, "converged": conv, "seconds": el, "threads": threads}
+
+
+def run_reference(args, cases, rank, world):
+    """Reference arm: the CPU restatement of PAGANI on every host core."""
+    if rank != 0:
+        return
+    total_pts = None
+    screen = json.load(open(os.path.join(ROOT, "tests", "golden", "config4_screen.json")))
+    import gpuintegration_gb300 as pg
+    lib = pg.load_library()
+    # evaluation count of the whole workload, from the screen run (leaf regions x points, x2 for inner nodes)
+    fe = [lib.pg_feval(c.integrand.ndim) for c in cases]
+    total_pts = float(sum(2 * n * f for n, f in zip(screen["nregions"][:len(cases)], fe)))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        s = cpu_leg(cases, args.cpu_seconds / 2)
+        if i >= args.warmup:
+            vals.append(s)
+    pps = sum(v["points_per_s"] for v in vals) / len(vals)
+    value = len(cases) / (total_pts / pps)
+    sample = f"first {vals[-1]['integrals']} integrals of the workload per step, extrapolated by evaluation count"
+    line = {"metric": METRIC, "value": value, "unit": "integrals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * vals[-1]["seconds"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "count": len(cases), "l2": "n/a (CPU)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "integrals/s", "cores": vals[-1]["threads"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "integrals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "no CPU PAGANI in the reference (Cuhre via cubacpp needs libcuba, absent); the oracle port "
+                    "restates the reference's CUDA iteration on host threads"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from gpuintegration_gb300 import workloads as W
+    cases = W.config4_cases(args.count)
+    if args.impl == "reference":
+        run_reference(args, cases, rank, world)
+        return
+
+    import torch
+    import gpuintegration_gb300 as pg
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ctx = pg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=f"cuda:{local}")
+    n = len(cases)
+    fs = (pg.PgIntegrand * n)(*[c.integrand.to_c() for c in cases])
+    eps = np.array([c.epsrel for c in cases])
+    opt = pg.default_options(max_regions=args.max_regions)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")  # > 129 MB L2
+
+    def step(completion=None):
+        return ctx.batch_integrate(fs, eps, 0.0, options=opt, completion_ms=completion)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    wall, conv_counts, lat = [], [], []
+    results = None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        comp = np.zeros(n)
+        ev0[k].record(stream)
+        t0 = time.perf_counter()
+        results = step(comp)
+        t1 = time.perf_counter()
+        ev1[k].record(stream)
+        wall.append(t1 - t0)
+        lat.append(comp)
+        conv_counts.append(sum(1 for c, r in zip(cases, results) if within(c, r)))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    dev_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    st = ctx.stats()
+    ctx.set_profiling(False)
+    dev_s = sum(dev_ms) / 1000.0
+    wall_s = sum(wall)
+    if dist:
+        t = torch.tensor([dev_s, wall_s], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall_s = float(t[0]), float(t[1])
+    converged = sum(conv_counts)
+    value = world * converged / dev_s
+    e2e = world * converged / wall_s
+    lat_all = np.concatenate(lat)
+    # Roofline of the dominant kernel (region evaluation, FP64 pipe).
+    alg = algorithmic_flops(cases, results) * args.steps
+    achieved = alg / (st.eval_ms / 1000.0) / 1e12
+    peak = ctx.probe_fp64_peak()
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "eval_kernel_dram.txt")
+    if os.path.exists(prof):
+        for line in open(prof):
+            if line.startswith("dram_bytes_per_eval_point:"):
+                per_pt = float(line.split(":")[1])
+                traffic = per_pt * (st.points_evaluated / max(st.eval_launches, 1))
+    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": "eval_kernel",
+            "peak_source": "measured FP64 FMA rate of this GPU (pg_probe_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
+            "algorithmic_flops_per_step": alg / args.steps,
+            "eval_ms_per_step": st.eval_ms / args.steps, "stage_ms_per_step": st.stage_ms / args.steps,
+            "stage_gbs": (st.stage_bytes / max(st.stage_ms, 1e-9)) / 1e6}
+    line = {"metric": METRIC, "value": value, "unit": "integrals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "count": n, "pool_regions": args.max_regions,
+                       "l2": "256 MB flush before every step", "seed": "config4_screen.json master 4096"},
+            "e2e": {"value": e2e, "unit": "integrals/s", "h2d_bytes_per_step": st.h2d_bytes // args.steps,
+                    "d2h_bytes_per_step": st.d2h_bytes // args.steps},
+            "gpu_launches": int(st.launches), "clocks": clk, "roofline": roof,
+            "latency_ms": {"p50": float(np.percentile(lat_all, 50)), "p99": float(np.percentile(lat_all, 99))},
+            "converged_per_step": conv_counts, "points_per_s": st.points_evaluated / dev_s,
+            "regions_per_step": st.regions_evaluated // args.steps}
+    if rank == 0:
+        # Plain per-call path on the same GPU, on a sample (batched on the same sample for the ratio).
+        ns = min(args.plain_sample, n)
+        sub = cases[:ns]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c in sub:
+            ctx.integrate(c.integrand, c.epsrel, 0.0)
+        plain_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctx.batch_integrate([c.integrand for c in sub], [c.epsrel for c in sub], 0.0, options=opt)
+        batch_s = time.perf_counter() - t0
+        line["plain"] = {"sample": ns, "plain_integrals_per_s": ns / plain_s, "batched_integrals_per_s": ns / batch_s,
+                         "batched_over_plain": plain_s / batch_s}
+        # CPU baseline: the oracle on all host cores, bounded sample, extrapolated by evaluation count.
+        cpu = cpu_leg(cases, args.cpu_seconds)
+        total_pts = sum(r.neval for r in results)
+        line["cpu_baseline"] = {"value": n / (total_pts / cpu["points_per_s"]), "unit": "integrals/s",
+                                "cores": cpu["threads"], "kind": "port",
+                                "sample": f"first {cpu['integrals']} integrals with <= {CPU_SAMPLE_MAX_REGIONS} regions "
+                                          f"({cpu['seconds']:.1f} s), throughput extrapolated to the whole step "
+                                          f"by evaluation count"}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

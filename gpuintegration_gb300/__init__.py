@@ -128,6 +128,9 @@ def load_library(path: str = LIB_PATH):
                                                P(PgMcubesOptions), P(PgResult)]),
         "pg_batch_integrate": (ctypes.c_int, [c_ctx, ctypes.c_uint64, P(PgIntegrand), _D, _D, P(PgOptions),
                                               P(PgResult)]),
+        "pg_batch_integrate_timed": (ctypes.c_int, [c_ctx, ctypes.c_uint64, P(PgIntegrand), _D, _D, P(PgOptions),
+                                                    P(PgResult), _D]),
+        "pg_probe_fp64_peak": (ctypes.c_int, [c_ctx, _D]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -278,15 +281,26 @@ class Context:
                                           ctypes.byref(o), ctypes.byref(r)))
         return IntegrationResult.from_c(r)
 
-    def batch_integrate(self, fs: Sequence[Integrand], epsrel, epsabs, options: Optional[PgOptions] = None):
+    def batch_integrate(self, fs: Sequence[Integrand], epsrel, epsabs, options: Optional[PgOptions] = None,
+                        completion_ms: Optional[np.ndarray] = None):
         n = len(fs)
-        arr = (PgIntegrand * n)(*[f.to_c() for f in fs])
+        arr = fs if isinstance(fs, ctypes.Array) else (PgIntegrand * n)(*[f.to_c() for f in fs])
         er = np.ascontiguousarray(np.broadcast_to(np.asarray(epsrel, dtype=np.float64), (n,)))
         ea = np.ascontiguousarray(np.broadcast_to(np.asarray(epsabs, dtype=np.float64), (n,)))
         out = (PgResult * n)()
         o = options if options is not None else default_options()
-        self._check(self.lib.pg_batch_integrate(self.h, n, arr, _ptr(er), _ptr(ea), ctypes.byref(o), out))
+        self._check(self.lib.pg_batch_integrate_timed(self.h, n, arr, _ptr(er), _ptr(ea), ctypes.byref(o), out,
+                                                      _ptr(completion_ms)))
         return [IntegrationResult.from_c(out[i]) for i in range(n)]
+
+    def probe_fp64_peak(self) -> float:
+        """Measured FP64 FMA rate of this GPU in TFLOP/s."""
+        v = ctypes.c_double()
+        self._check(self.lib.pg_probe_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value
+
+    def stream_handle(self) -> int:
+        return self.lib.pg_context_stream(self.h) or 0
 
     def evaluate_regions(self, f: Integrand, left: np.ndarray, length: np.ndarray, vol: Optional[Volume] = None,
                          eval_mode: int = 0):

@@ -92,6 +92,23 @@ __global__ void flag_offsets_kernel(const uint8_t* __restrict__ f, uint64_t n, c
     }
 }
 
+// Eight independent FMA chains per thread (FP64 issue-rate probe).
+__global__ void fp64_fma_probe_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = __fma_rn(x0, a, b);
+    x1 = __fma_rn(x1, a, b);
+    x2 = __fma_rn(x2, a, b);
+    x3 = __fma_rn(x3, a, b);
+    x4 = __fma_rn(x4, a, b);
+    x5 = __fma_rn(x5, a, b);
+    x6 = __fma_rn(x6, a, b);
+    x7 = __fma_rn(x7, a, b);
+  }
+  const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678) out[0] = s;  // keeps the chains alive
+}
+
 struct Guard {
   explicit Guard(pg_context* c) : lk(c->mu) { cudaSetDevice(c->eng->device); }
   std::lock_guard<std::mutex> lk;
@@ -213,6 +230,11 @@ int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double e
 
 int pg_batch_integrate(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
                        const double* epsabs, const pg_options* opt, pg_result* out) {
+  return pg_batch_integrate_timed(ctx, count, fs, epsrel, epsabs, opt, out, nullptr);
+}
+
+int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
+                             const double* epsabs, const pg_options* opt, pg_result* out, double* completion_ms) {
   if (!ctx || (!fs && count) || !epsrel || !epsabs || (!out && count)) return set_err(ctx, PG_BAD_ARG, "null argument");
   if (count > 0xffffffffull) return set_err(ctx, PG_BAD_ARG, "too many integrands");
   Guard g(ctx);
@@ -228,9 +250,14 @@ int pg_batch_integrate(pg_context* ctx, uint64_t count, const pg_integrand* fs, 
     if (opt) jobs[i].opt = *opt; else pg_options_default(&jobs[i].opt);
     if (jobs[i].opt.max_iters <= 0) jobs[i].opt.max_iters = 700;
   }
-  int rc = ctx->eng->run(jobs, pg::launch_family_eval);
+  pg::RunPolicy pol;
+  if (opt) pol.max_regions = opt->max_regions;
+  int rc = ctx->eng->run(jobs, pg::launch_family_eval, pol);
   if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
-  for (uint64_t i = 0; i < count; ++i) out[i] = jobs[i].res;
+  for (uint64_t i = 0; i < count; ++i) {
+    out[i] = jobs[i].res;
+    if (completion_ms) completion_ms[i] = jobs[i].done_ms;
+  }
   return PG_OK;
 }
 
@@ -400,13 +427,13 @@ int pg_filter_split(pg_context* ctx, int ndim, uint64_t n, const double* left, c
           (const pg::ChunkRef*)ctx->s_chunks.p, (const pg::SegDesc*)ctx->s_seg.p, (const pg::Transition*)ctx->s_trans.p,
           off, (const pg::IntegralDesc*)ctx->s_desc.p, (const uint8_t*)ctx->s_act.p, (const double*)ctx->s_left.p,
           (const double*)ctx->s_len.p, n, (const int32_t*)ctx->s_bis.p, val, (double*)ctx->s_out_left.p,
-          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out);
+          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out, 0u);
     else
       pg::compact_split_kernel<16><<<(unsigned)nch, pg::kRedThreads, 0, s>>>(
           (const pg::ChunkRef*)ctx->s_chunks.p, (const pg::SegDesc*)ctx->s_seg.p, (const pg::Transition*)ctx->s_trans.p,
           off, (const pg::IntegralDesc*)ctx->s_desc.p, (const uint8_t*)ctx->s_act.p, (const double*)ctx->s_left.p,
           (const double*)ctx->s_len.p, n, (const int32_t*)ctx->s_bis.p, val, (double*)ctx->s_out_left.p,
-          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out);
+          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out, 0u);
     ctx->eng->stats.launches++;
   };
   launch((const double*)ctx->s_est.p, (double*)ctx->s_par.p);
@@ -494,6 +521,33 @@ int do_integration_from_c(double* res) {
   if (rc < 0) return rc;
   if (r.status == 0) *res = r.estimate;
   return r.status;
+}
+
+int pg_probe_fp64_peak(pg_context* ctx, double* tflops) {
+  if (!ctx || !tflops) return set_err(ctx, PG_BAD_ARG, "null argument");
+  Guard g(ctx);
+  CAPI_ENSURE(ctx, ctx->s_res, 8);
+  cudaStream_t s = ctx->eng->stream();
+  cudaEvent_t a, b;
+  CAPI_TRY(ctx, cudaEventCreate(&a), "event");
+  CAPI_TRY(ctx, cudaEventCreate(&b), "event");
+  const int blocks = ctx->eng->num_sms * 8, threads = 256, iters = 4096;
+  double best = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(a, s);
+    fp64_fma_probe_kernel<<<blocks, threads, 0, s>>>((double*)ctx->s_res.p, iters, 0.999999, 1e-7);
+    cudaEventRecord(b, s);
+    CAPI_TRY(ctx, cudaEventSynchronize(b), "probe");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    const double tf = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    if (rep > 0 && tf > best) best = tf;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->eng->stats.launches += 3;
+  *tflops = best;
+  return PG_OK;
 }
 
 // ---------------- m-Cubes ----------------

@@ -2,6 +2,7 @@
 #include "pg_engine.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -376,23 +377,117 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
   return PG_OK;
 }
 
-int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch) {
+// Grows region list `which` to hold `need` regions with `rows` rows, keeping
+// its first `live` regions (and `live_par` parent estimates).
+int Engine::grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_t live_par) {
+  int rc;
+  if (reg_cap_[which] < need || reg_rows_[which] < rows) {
+    const uint64_t cap = std::max<uint64_t>(std::max<uint64_t>(need, reg_cap_[which] + reg_cap_[which] / 2), 4096);
+    const int r = std::max(rows, reg_rows_[which]);
+    PG_TRY(cudaStreamSynchronize(stream_), "stream sync before reallocation");
+    DevBuf nl, nn, no;
+    PG_TRY(cudaMalloc(&nl.p, cap * r * 8), "cudaMalloc region list");
+    nl.bytes = cap * r * 8;
+    if (cudaMalloc(&nn.p, cap * r * 8) != cudaSuccess) {
+      cudaFree(nl.p);
+      return fail(cudaErrorMemoryAllocation, "cudaMalloc region list");
+    }
+    nn.bytes = cap * r * 8;
+    if (cudaMalloc(&no.p, cap * 4) != cudaSuccess) {
+      cudaFree(nl.p);
+      cudaFree(nn.p);
+      return fail(cudaErrorMemoryAllocation, "cudaMalloc region owners");
+    }
+    no.bytes = cap * 4;
+    if (live) {
+      const int old_rows = reg_rows_[which];
+      PG_TRY(cudaMemcpy2DAsync(nl.p, cap * 8, left_[which].p, reg_cap_[which] * 8, live * 8, old_rows,
+                               cudaMemcpyDeviceToDevice, stream_), "grow copy");
+      PG_TRY(cudaMemcpy2DAsync(nn.p, cap * 8, len_[which].p, reg_cap_[which] * 8, live * 8, old_rows,
+                               cudaMemcpyDeviceToDevice, stream_), "grow copy");
+      PG_TRY(cudaMemcpyAsync(no.p, owner_[which].p, live * 4, cudaMemcpyDeviceToDevice, stream_), "grow copy");
+      PG_TRY(cudaStreamSynchronize(stream_), "grow copy");
+    }
+    if (left_[which].p) cudaFree(left_[which].p);
+    if (len_[which].p) cudaFree(len_[which].p);
+    if (owner_[which].p) cudaFree(owner_[which].p);
+    left_[which] = nl;
+    len_[which] = nn;
+    owner_[which] = no;
+    reg_cap_[which] = cap;
+    reg_rows_[which] = r;
+  }
+  // Parent estimates: at most one per region.
+  if (parent_[which].bytes < need * 8) {
+    DevBuf np;
+    const size_t bytes = std::max<size_t>(need * 8, parent_[which].bytes + parent_[which].bytes / 2);
+    PG_TRY(cudaStreamSynchronize(stream_), "stream sync before reallocation");
+    PG_TRY(cudaMalloc(&np.p, bytes), "cudaMalloc parents");
+    np.bytes = bytes;
+    if (live_par) PG_TRY(cudaMemcpyAsync(np.p, parent_[which].p, live_par * 8, cudaMemcpyDeviceToDevice, stream_),
+                         "grow copy");
+    PG_TRY(cudaStreamSynchronize(stream_), "grow copy");
+    if (parent_[which].p) cudaFree(parent_[which].p);
+    parent_[which] = np;
+  }
+  (void)rc;
+  return PG_OK;
+}
+
+int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
+                    uint64_t out_stride, uint32_t* out_owner, double* parent_out) {
+  (void)nxt;
+  if (nchunks == 0) return PG_OK;
+  if (maxd <= 8) {
+    compact_split_kernel<8><<<nchunks, kRedThreads, 0, stream_>>>(
+        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
+        (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
+        (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
+        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0);
+  } else {
+    compact_split_kernel<16><<<nchunks, kRedThreads, 0, stream_>>>(
+        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
+        (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
+        (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
+        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0);
+  }
+  stats.launches++;
+  PG_TRY(cudaGetLastError(), "compact/split launch");
+  return PG_OK;
+}
+
+int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPolicy& policy) {
   int rc;
   PG_TRY(cudaSetDevice(device), "cudaSetDevice");
   const uint32_t njobs = (uint32_t)jobs.size();
   if (njobs == 0) return PG_OK;
   int maxd = 2;
   for (auto& J : jobs) maxd = std::max(maxd, J.desc.d);
+  // Pool capacity in regions: both region lists, owners, parents and the
+  // per-region scratch of one iteration.
+  const uint64_t bytes_per_region = 32ull * maxd + 53;
+  uint64_t cap = policy.max_regions;
+  if (cap == 0) {
+    size_t fr = 0, tot = 0;
+    PG_TRY(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    cap = (uint64_t)(0.6 * (double)fr) / bytes_per_region;
+  }
+  cap = std::max<uint64_t>(cap, 4096);
+  const uint64_t admit_limit = (uint64_t)(policy.admit_fraction * (double)cap);
   // Per-integral arrays.
   if ((rc = ensure(descs_, njobs * sizeof(IntegralDesc))) != PG_OK) return rc;
   if ((rc = ensure(segs_, njobs * sizeof(SegDesc))) != PG_OK) return rc;
   if ((rc = ensure(trans_, njobs * sizeof(Transition))) != PG_OK) return rc;
   if ((rc = ensure(scal_, njobs * sizeof(IterScalars))) != PG_OK) return rc;
   if ((rc = ensure(live_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
+  if ((rc = ensure(adm_starts_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
+  if ((rc = ensure(adm_ids_, (njobs + 1) * sizeof(uint32_t))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_segs_, njobs * sizeof(SegDesc))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_trans_, njobs * sizeof(Transition))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_scal_, njobs * sizeof(IterScalars))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_live_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_adm_starts_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_adm_ids_, (njobs + 1) * sizeof(uint32_t))) != PG_OK) return rc;
   {
     std::vector<IntegralDesc> descs(njobs);
     for (uint32_t j = 0; j < njobs; ++j) descs[j] = jobs[j].desc;
@@ -401,66 +496,113 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch) {
     PG_TRY(cudaStreamSynchronize(stream_), "desc upload");
     stats.h2d_bytes += njobs * sizeof(IntegralDesc);
   }
-  // Initial uniform split of every integral, one launch for the batch.
-  uint64_t total = 0;
-  {
-    uint64_t* starts = (uint64_t*)h_live_.p;
-    for (uint32_t j = 0; j < njobs; ++j) {
-      Job& J = jobs[j];
-      J.res = pg_result{};
-      J.res.status = 1;
-      J.res.last_phase = -1;
-      J.cls = ClassifierState{};
-      J.cls.epsrel = J.epsrel;
-      J.cls.epsabs = J.epsabs;
-      J.cls.required_digits = (int)std::ceil(std::log10(1 / J.epsrel));
-      J.cls.ndim = J.desc.d;
-      J.cls.total_mem = J.opt.device_mem_model > 0 ? J.opt.device_mem_model : 16e9;
-      J.n = ipow_u((uint64_t)parts_for(J.desc.d), J.desc.d);
-      J.start = total;
-      J.par_start = 0;
-      J.has_parent = 0;
-      J.iters = 0;
-      J.done = false;
-      starts[j] = total;
-      total += J.n;
-    }
-    starts[njobs] = total;
-    if ((rc = ensure(left_[0], total * maxd * 8)) != PG_OK) return rc;
-    if ((rc = ensure(len_[0], total * maxd * 8)) != PG_OK) return rc;
-    if ((rc = ensure(owner_[0], total * 4)) != PG_OK) return rc;
-    reg_cap_[0] = left_[0].bytes / (maxd * 8);
-    reg_cap_[0] = std::min(reg_cap_[0], len_[0].bytes / (maxd * 8));
-    reg_rows_[0] = maxd;
-    PG_TRY(cudaMemcpyAsync(live_.p, starts, (njobs + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, stream_),
-           "start upload");
-    uniform_split_batch_kernel<<<(unsigned)div_up(total, 256), 256, 0, stream_>>>(
-        (double*)left_[0].p, (double*)len_[0].p, reg_cap_[0], (uint32_t*)owner_[0].p, (const uint64_t*)live_.p,
-        (const IntegralDesc*)descs_.p, njobs);
-    stats.launches++;
-    PG_TRY(cudaGetLastError(), "uniform split launch");
-    PG_TRY(cudaStreamSynchronize(stream_), "uniform split");
+  for (uint32_t j = 0; j < njobs; ++j) {
+    Job& J = jobs[j];
+    J.res = pg_result{};
+    J.res.status = 1;
+    J.res.last_phase = -1;
+    J.cls = ClassifierState{};
+    J.cls.epsrel = J.epsrel;
+    J.cls.epsabs = J.epsabs;
+    J.cls.required_digits = (int)std::ceil(std::log10(1 / J.epsrel));
+    J.cls.ndim = J.desc.d;
+    J.cls.total_mem = J.opt.device_mem_model > 0 ? J.opt.device_mem_model : 16e9;
+    J.n = ipow_u((uint64_t)parts_for(J.desc.d), J.desc.d);
+    J.start = J.par_start = 0;
+    J.has_parent = 0;
+    J.iters = 0;
+    J.done = false;
+    J.state = JOB_PENDING;
+    J.sp_left.clear();
+    J.sp_len.clear();
+    J.sp_par.clear();
   }
+  const auto t_start = std::chrono::steady_clock::now();
   int cur = 0;
+  uint64_t T = 0, P = 0;  // regions and parent estimates in the current list
+  uint32_t first_waiting = 0;
   std::vector<uint32_t> live;
   std::vector<ChunkRef> chunk_list;
   std::vector<int> mode(njobs);
   std::vector<uint64_t> keepA(njobs);
+  std::vector<uint32_t> adm_pending;
   while (true) {
+    // ---- admission: waiting integrals join at the end of the list, in order
+    adm_pending.clear();
+    {
+      uint64_t t = T, pp = P;
+      uint64_t* hs = (uint64_t*)h_adm_starts_.p;
+      uint32_t* hi = (uint32_t*)h_adm_ids_.p;
+      std::vector<uint32_t> restore;
+      while (first_waiting < njobs && jobs[first_waiting].state == JOB_DONE) ++first_waiting;
+      for (uint32_t j = first_waiting; j < njobs; ++j) {
+        Job& J = jobs[j];
+        if (J.state != JOB_PENDING && J.state != JOB_SPILLED) continue;
+        if (t + J.n > admit_limit && t > 0) break;
+        J.start = t;
+        J.par_start = pp;
+        t += J.n;
+        if (J.state == JOB_SPILLED) {
+          pp += J.n / 2;
+          restore.push_back(j);
+        } else {
+          hs[adm_pending.size()] = J.start;
+          hi[adm_pending.size()] = j;
+          adm_pending.push_back(j);
+        }
+        J.state = JOB_RESIDENT;
+      }
+      if (t > T) {
+        if ((rc = grow_list(cur, t, maxd, T, P)) != PG_OK) return rc;
+        if (!adm_pending.empty()) {
+          const uint32_t m = (uint32_t)adm_pending.size();
+          hs[m] = jobs[adm_pending.back()].start + jobs[adm_pending.back()].n;
+          PG_TRY(cudaMemcpyAsync(adm_starts_.p, hs, (m + 1) * 8, cudaMemcpyHostToDevice, stream_), "admit upload");
+          PG_TRY(cudaMemcpyAsync(adm_ids_.p, hi, m * 4, cudaMemcpyHostToDevice, stream_), "admit upload");
+          const uint64_t span = hs[m] - hs[0];
+          uniform_split_batch_kernel<<<(unsigned)div_up(span, 256), 256, 0, stream_>>>(
+              (double*)left_[cur].p, (double*)len_[cur].p, reg_cap_[cur], (uint32_t*)owner_[cur].p,
+              (const uint64_t*)adm_starts_.p, (const uint32_t*)adm_ids_.p, (const IntegralDesc*)descs_.p, m);
+          stats.launches++;
+          PG_TRY(cudaGetLastError(), "uniform split launch");
+        }
+        for (uint32_t j : restore) {
+          Job& J = jobs[j];
+          const int d = J.desc.d;
+          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, J.sp_left.data(), J.n * 8,
+                                   J.n * 8, d, cudaMemcpyHostToDevice, stream_), "restore");
+          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, J.sp_len.data(), J.n * 8,
+                                   J.n * 8, d, cudaMemcpyHostToDevice, stream_), "restore");
+          PG_TRY(cudaMemcpyAsync((double*)parent_[cur].p + J.par_start, J.sp_par.data(), (J.n / 2) * 8,
+                                 cudaMemcpyHostToDevice, stream_), "restore");
+          fill_owner_kernel<<<(unsigned)div_up(J.n, 256), 256, 0, stream_>>>((uint32_t*)owner_[cur].p, J.start, J.n,
+                                                                            j);
+          stats.launches++;
+          PG_TRY(cudaGetLastError(), "restore launch");
+          stats.h2d_bytes += J.n * 16 * d + J.n * 4;
+          PG_TRY(cudaStreamSynchronize(stream_), "restore");  // host copies may be released now
+          std::vector<double>().swap(J.sp_left);
+          std::vector<double>().swap(J.sp_len);
+          std::vector<double>().swap(J.sp_par);
+        }
+        T = t;
+        P = pp;
+      }
+    }
     live.clear();
     for (uint32_t j = 0; j < njobs; ++j)
-      if (!jobs[j].done) live.push_back(j);
+      if (jobs[j].state == JOB_RESIDENT) live.push_back(j);
     if (live.empty()) break;
-    // Segments and chunk list of the live integrals.
+    // Segments and chunk list of the resident integrals.
     chunk_list.clear();
     SegDesc* hs = (SegDesc*)h_segs_.p;
-    uint64_t N = 0;
     for (uint32_t j = 0; j < njobs; ++j) {
       Job& J = jobs[j];
       SegDesc S;
       std::memset(&S, 0, sizeof S);
+      const bool res = J.state == JOB_RESIDENT;
       S.start = J.start;
-      S.n = J.done ? 0 : J.n;
+      S.n = res ? J.n : 0;
       S.par_start = J.par_start;
       S.chunk_start = (uint32_t)chunk_list.size();
       S.nchunks = (uint32_t)div_up(S.n, kChunk);
@@ -469,8 +611,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch) {
       S.epsrel = J.epsrel;
       for (uint32_t b = 0; b < S.nchunks; ++b) chunk_list.push_back(ChunkRef{j, b});
       hs[j] = S;
-      if (!J.done) N = std::max(N, J.start + J.n);
     }
+    const uint64_t N = T;
     const uint64_t nchunks = chunk_list.size();
     if ((rc = ensure(est_, N * 8)) != PG_OK) return rc;
     if ((rc = ensure(err_a_, N * 8)) != PG_OK) return rc;
@@ -518,6 +660,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch) {
     if (profiling) {
       record(ev_[0], ev_[1], &stats.eval_ms);
       record(ev_[1], ev_[2], &stats.stage_ms);
+      if (compact_timing_pending_) record(ev_[2 + 2], ev_[3 + 2], &stats.stage_ms);
+      compact_timing_pending_ = false;
     }
     const IterScalars* sc = (const IterScalars*)h_scal_.p;
     // Host decisions, per integral, exactly as Workspace::integrate.
@@ -597,78 +741,104 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch) {
       mode[j] = m;
       keepA[j] = A;
     }
-    // Layout of the next list.
+    const double now_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    for (uint32_t j : live)
+      if (jobs[j].done) {
+        jobs[j].state = JOB_DONE;
+        jobs[j].done_ms = now_ms;
+      }
+    // ---- placement of the next list: in order, while the pool has room;
+    // the rest leave the pool with their next list in host memory.
     Transition* ht = (Transition*)h_trans_.p;
     uint64_t out_total = 0, par_total = 0;
+    std::vector<uint32_t> spill;
     for (uint32_t j = 0; j < njobs; ++j) {
-      Transition T;
-      std::memset(&T, 0, sizeof T);
-      const bool go = !jobs[j].done && mode[j] != 0;
-      if (go) {
-        T.mode = mode[j];
-        T.A = keepA[j];
-        T.out_start = out_total;
-        T.par_out = par_total;
-        out_total += 2 * keepA[j];
-        par_total += keepA[j];
+      Transition Tr;
+      std::memset(&Tr, 0, sizeof Tr);
+      Job& J = jobs[j];
+      if (J.state == JOB_RESIDENT && mode[j] != 0) {
+        Tr.mode = mode[j];
+        Tr.A = keepA[j];
+        if (out_total + 2 * keepA[j] <= cap || out_total == 0) {
+          Tr.out_start = out_total;
+          Tr.par_out = par_total;
+          out_total += 2 * keepA[j];
+          par_total += keepA[j];
+        } else {
+          spill.push_back(j);
+        }
       }
-      ht[j] = T;
+      ht[j] = Tr;
     }
-    if (out_total == 0) continue;  // every integral finished this iteration
-    const int nxt = cur ^ 1;
-    if (reg_cap_[nxt] < out_total || reg_rows_[nxt] < maxd) {
-      const uint64_t cap = std::max<uint64_t>(out_total + out_total / 2, 1024);
-      PG_TRY(cudaStreamSynchronize(stream_), "stream sync before reallocation");
-      if (left_[nxt].p) cudaFree(left_[nxt].p), left_[nxt] = DevBuf{};
-      if (len_[nxt].p) cudaFree(len_[nxt].p), len_[nxt] = DevBuf{};
-      if ((rc = ensure(left_[nxt], cap * maxd * 8)) != PG_OK) return rc;
-      if ((rc = ensure(len_[nxt], cap * maxd * 8)) != PG_OK) return rc;
-      reg_cap_[nxt] = cap;
-      reg_rows_[nxt] = maxd;
-    }
-    if ((rc = ensure(owner_[nxt], out_total * 4)) != PG_OK) return rc;
-    if ((rc = ensure(parent_[nxt], par_total * 8)) != PG_OK) return rc;
     PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
            "transition upload");
     stats.h2d_bytes += njobs * sizeof(Transition);
-    if (profiling) cudaEventRecord(ev_[2], stream_);
-    const uint64_t out_stride = reg_cap_[nxt];
-    if (maxd <= 8) {
-      compact_split_kernel<8><<<(unsigned)nchunks, kRedThreads, 0, stream_>>>(
-          (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
-          (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
-          (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
-          (const double*)est_.p, (double*)left_[nxt].p, (double*)len_[nxt].p, out_stride, (uint32_t*)owner_[nxt].p,
-          (double*)parent_[nxt].p);
-    } else {
-      compact_split_kernel<16><<<(unsigned)nchunks, kRedThreads, 0, stream_>>>(
-          (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
-          (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
-          (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
-          (const double*)est_.p, (double*)left_[nxt].p, (double*)len_[nxt].p, out_stride, (uint32_t*)owner_[nxt].p,
-          (double*)parent_[nxt].p);
-    }
-    stats.launches++;
-    PG_TRY(cudaGetLastError(), "compact/split launch");
-    if (profiling) {
-      cudaEventRecord(ev_[3], stream_);
-      PG_TRY(cudaEventSynchronize(ev_[3]), "compact/split");
-      record(ev_[2], ev_[3], &stats.stage_ms);
-    }
-    for (uint32_t j = 0; j < njobs; ++j) {
-      const Transition& T = ht[j];
-      if (jobs[j].done || T.mode == 0) continue;
+    // Spilled integrals: children into a transient buffer, then to host memory.
+    for (uint32_t j : spill) {
       Job& J = jobs[j];
-      stats.stage_bytes += J.n + T.A * (uint64_t)(16 * J.desc.d + 12) + 2 * T.A * (uint64_t)(16 * J.desc.d + 4) +
-                           T.A * 8;
-      J.start = T.out_start;
-      J.n = 2 * T.A;
-      J.par_start = T.par_out;
+      const SegDesc& S = hs[j];
+      const uint64_t A = keepA[j], n2 = 2 * A;
+      const int d = J.desc.d;
+      if ((rc = ensure(sp_left_, n2 * maxd * 8)) != PG_OK) return rc;
+      if ((rc = ensure(sp_len_, n2 * maxd * 8)) != PG_OK) return rc;
+      if ((rc = ensure(sp_par_, A * 8)) != PG_OK) return rc;
+      // This job's transition must place it at offset 0 of the transient buffer.
+      Transition Tr = ht[j];
+      Tr.out_start = 0;
+      Tr.par_out = 0;
+      PG_TRY(cudaMemcpyAsync((Transition*)trans_.p + j, &Tr, sizeof Tr, cudaMemcpyHostToDevice, stream_),
+             "transition upload");
+      if ((rc = compact(cur, cur ^ 1, S.chunk_start, S.nchunks, maxd, (double*)sp_left_.p, (double*)sp_len_.p, n2,
+                        nullptr, (double*)sp_par_.p)) != PG_OK)
+        return rc;
+      J.sp_left.resize(n2 * d);
+      J.sp_len.resize(n2 * d);
+      J.sp_par.resize(A);
+      PG_TRY(cudaMemcpyAsync(J.sp_left.data(), sp_left_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+      PG_TRY(cudaMemcpyAsync(J.sp_len.data(), sp_len_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+      PG_TRY(cudaMemcpyAsync(J.sp_par.data(), sp_par_.p, A * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+      PG_TRY(cudaStreamSynchronize(stream_), "spill");
+      stats.d2h_bytes += n2 * d * 16 + A * 8;
+      Tr.mode = 0;  // not part of the resident compaction below
+      ht[j] = Tr;
+      PG_TRY(cudaMemcpyAsync((Transition*)trans_.p + j, &ht[j], sizeof Tr, cudaMemcpyHostToDevice, stream_),
+             "transition upload");
+      PG_TRY(cudaStreamSynchronize(stream_), "transition upload");
+      J.state = JOB_SPILLED;
+      J.n = n2;
       J.has_parent = 1;
     }
+    const int nxt = cur ^ 1;
+    if (out_total > 0) {
+      if ((rc = grow_list(nxt, out_total, maxd, 0, 0)) != PG_OK) return rc;
+      if (profiling) cudaEventRecord(ev_[4], stream_);
+      if ((rc = compact(cur, nxt, 0, (uint32_t)nchunks, maxd, (double*)left_[nxt].p, (double*)len_[nxt].p,
+                        reg_cap_[nxt], (uint32_t*)owner_[nxt].p, (double*)parent_[nxt].p)) != PG_OK)
+        return rc;
+      if (profiling) {
+        cudaEventRecord(ev_[5], stream_);
+        compact_timing_pending_ = true;  // read after the next synchronisation
+      }
+    }
+    for (uint32_t j = 0; j < njobs; ++j) {
+      const Transition& Tr = ht[j];
+      Job& J = jobs[j];
+      if (J.state != JOB_RESIDENT || Tr.mode == 0) continue;
+      stats.stage_bytes += J.n + Tr.A * (uint64_t)(16 * J.desc.d + 12) + 2 * Tr.A * (uint64_t)(16 * J.desc.d + 4) +
+                           Tr.A * 8;
+      J.start = Tr.out_start;
+      J.n = 2 * Tr.A;
+      J.par_start = Tr.par_out;
+      J.has_parent = 1;
+    }
+    T = out_total;
+    P = par_total;
     cur = nxt;
   }
   PG_TRY(cudaStreamSynchronize(stream_), "run");
+  if (profiling && compact_timing_pending_) record(ev_[4], ev_[5], &stats.stage_ms);
+  compact_timing_pending_ = false;
   return PG_OK;
 }
 

@@ -63,6 +63,8 @@ struct ClassifierState {
   bool criteria_met(uint64_t n) const;
 };
 
+enum JobState { JOB_PENDING = 0, JOB_RESIDENT = 1, JOB_SPILLED = 2, JOB_DONE = 3 };
+
 struct Job {
   IntegralDesc desc{};
   double epsrel = 1e-3, epsabs = 1e-12;
@@ -76,6 +78,17 @@ struct Job {
   int iters = 0;
   bool done = false;
   int error = 0;
+  int state = JOB_PENDING;
+  double done_ms = 0.0;  // host time from the start of the run to the iteration that finished it
+  // Next region list of a job moved out of the device pool (host copy):
+  // rows [dim][n] of left and length, and the n/2 parent estimates.
+  std::vector<double> sp_left, sp_len, sp_par;
+};
+
+// Scheduling limits of one run.
+struct RunPolicy {
+  uint64_t max_regions = 0;   // pool capacity in regions (0: from free device memory)
+  double admit_fraction = 0.5;  // new work is admitted while the list is below this share of the pool
 };
 
 // Prepares an IntegralDesc from the C ABI description (host, no contraction).
@@ -93,7 +106,7 @@ class Engine {
   int init(std::string* why);
 
   // Runs every job to completion.  Returns PG_OK or a negative pg_status.
-  int run(std::vector<Job>& jobs, const EvalLauncher& launch);
+  int run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPolicy& policy = RunPolicy());
 
   // Evaluates caller-given regions (device pointers, SoA stride n).
   int evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length, uint64_t stride,
@@ -116,6 +129,9 @@ class Engine {
   int classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err, bool* ok, double* fin_est_out,
                    double* fin_err_out, uint64_t* num_active, double iter_est);
   int threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5]);
+  int grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_t live_par);
+  int compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
+              uint64_t out_stride, uint32_t* out_owner, double* parent_out);
   void record(cudaEvent_t a, cudaEvent_t b, double* acc);
 
   cudaStream_t stream_ = nullptr;
@@ -130,10 +146,13 @@ class Engine {
   // per-chunk
   DevBuf partials_, chunk_off_, chunks_;
   // per-integral
-  DevBuf segs_, trans_, descs_, scal_, live_, thr_out_;
+  DevBuf segs_, trans_, descs_, scal_, live_, thr_out_, adm_starts_, adm_ids_;
+  // transient device copy of one job's next list on its way to host memory
+  DevBuf sp_left_, sp_len_, sp_par_;
+  bool compact_timing_pending_ = false;
   // pinned host mirrors
-  DevBuf h_segs_, h_chunks_, h_trans_, h_scal_, h_live_, h_thr_;
-  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+  DevBuf h_segs_, h_chunks_, h_trans_, h_scal_, h_live_, h_thr_, h_adm_starts_, h_adm_ids_;
+  cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 }  // namespace pg

@@ -55,6 +55,35 @@ __device__ __forceinline__ double ipow_dev(double s, int e) {
   return r;
 }
 
+// Families that are products of per-axis factors h_k(x_k).  A region's
+// points take only 11 coordinate values per axis, so the evaluation kernel
+// computes each factor once per region and forms every point's value as the
+// product of its axes' factors (same operations, same order, same value).
+__host__ __device__ __forceinline__ bool family_separable(int family) {
+  return family == FAM_PRODUCT_PEAK || family == FAM_GAUSSIAN || family == FAM_C0 || family == FAM_DISCONTINUOUS ||
+         family == FAM_PRODUCT;
+}
+
+__device__ __forceinline__ double family_factor(const IntegralDesc& D, int k, double x) {
+  switch (D.family) {
+    case FAM_PRODUCT_PEAK: {
+      const double t = __dsub_rn(x, D.u[k]);
+      return __ddiv_rn(1.0, __fma_rn(t, t, D.ia2[k]));
+    }
+    case FAM_GAUSSIAN: {
+      const double q = __dmul_rn(D.a[k], __dsub_rn(x, D.u[k]));
+      return exp(-__dmul_rn(q, q));
+    }
+    case FAM_C0:
+      return exp(-__dmul_rn(D.a[k], fabs(__dsub_rn(x, D.u[k]))));
+    case FAM_DISCONTINUOUS:
+      return (x > D.u[k]) ? 0.0 : exp(__dmul_rn(D.a[k], x));
+    case FAM_PRODUCT:
+      return x;
+  }
+  return 1.0;
+}
+
 template <int MAXD>
 __device__ __forceinline__ double family_eval(const IntegralDesc& D, const double* x) {
   const int d = D.d;
@@ -69,15 +98,10 @@ __device__ __forceinline__ double family_eval(const IntegralDesc& D, const doubl
       return cos(s);
     }
     case FAM_PRODUCT_PEAK: {
-      double v = 1.0;
+      double v = family_factor(D, 0, x[0]);
 #pragma unroll
-      for (int i = 0; i < MAXD; ++i) {
-        if (i < d) {
-          const double t = __dsub_rn(x[i], D.u[i]);
-          const double term = __ddiv_rn(1.0, __fma_rn(t, t, D.ia2[i]));
-          v = (i == 0) ? term : __dmul_rn(v, term);
-        }
-      }
+      for (int i = 1; i < MAXD; ++i)
+        if (i < d) v = __dmul_rn(v, family_factor(D, i, x[i]));
       return v;
     }
     case FAM_CORNER_PEAK: {
@@ -87,35 +111,15 @@ __device__ __forceinline__ double family_eval(const IntegralDesc& D, const doubl
         if (i < d) s = __fma_rn(D.a[i], x[i], s);
       return __ddiv_rn(1.0, ipow_dev(s, d + 1));
     }
-    case FAM_GAUSSIAN: {
-      double s = 0.0;
-#pragma unroll
-      for (int i = 0; i < MAXD; ++i) {
-        if (i < d) {
-          const double q = __dmul_rn(D.a[i], __dsub_rn(x[i], D.u[i]));
-          s = __fma_rn(q, q, s);
-        }
-      }
-      return exp(-s);
-    }
-    case FAM_C0: {
-      double s = 0.0;
-#pragma unroll
-      for (int i = 0; i < MAXD; ++i)
-        if (i < d) s = __fma_rn(D.a[i], fabs(__dsub_rn(x[i], D.u[i])), s);
-      return exp(-s);
-    }
+    case FAM_GAUSSIAN:
+    case FAM_C0:
     case FAM_DISCONTINUOUS: {
-      bool out = false;
+      // Product of per-axis factors, axis 0 first.
+      double v = family_factor(D, 0, x[0]);
 #pragma unroll
-      for (int i = 0; i < MAXD; ++i)
-        if (i < d) out = out || (x[i] > D.u[i]);
-      if (out) return 0.0;
-      double s = 0.0;
-#pragma unroll
-      for (int i = 0; i < MAXD; ++i)
-        if (i < d) s = __fma_rn(D.a[i], x[i], s);
-      return exp(s);
+      for (int i = 1; i < MAXD; ++i)
+        if (i < d) v = __dmul_rn(v, family_factor(D, i, x[i]));
+      return v;
     }
     case FAM_PRODUCT: {
       double v = x[0];
@@ -149,6 +153,10 @@ struct FamilyFn {
   template <int MAXD>
   __device__ __forceinline__ double eval(const IntegralDesc& D, const double* x) const {
     return family_eval<MAXD>(D, x);
+  }
+  __device__ __forceinline__ bool separable(const IntegralDesc& D) const { return family_separable(D.family); }
+  __device__ __forceinline__ double factor(const IntegralDesc& D, int k, double x) const {
+    return family_factor(D, k, x);
   }
 };
 

@@ -91,6 +91,7 @@ template <int MAXD>
 struct EvalWarpSmem {
   IntegralDesc desc;
   double tab[MAXD * kCodesPerDim];
+  double fac[MAXD * kCodesPerDim];  // per-axis factors of separable integrands
   double fv[64];
   double lo[MAXD];
   double up[MAXD];
@@ -145,6 +146,9 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
       const double t = __fma_rn(rule.A[c], S.lo[k], __dmul_rn(rule.B[c], S.up[k]));
       S.tab[v] = S.desc.unit ? t : __fma_rn(t, S.desc.range[k], S.desc.glo[k]);
     }
+    const bool sep = fn.separable(S.desc);
+    if (sep)
+      for (int v = lane; v < d * kCodesPerDim; v += 32) S.fac[v] = fn.factor(S.desc, v / kCodesPerDim, S.tab[v]);
     __syncwarp();
     const double jac = S.desc.jac;
     double sa0 = 0, sa1 = 0, sa2 = 0, sa3 = 0, sa4 = 0;
@@ -155,10 +159,19 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
         const int p = base + half * 32 + lane;
         if (p < feval) {
           const uint64_t code = __ldg(&codes[p]);
-          double x[MAXD];
+          double f;
+          if (sep) {
+            f = S.fac[(int)(code & 15u)];
 #pragma unroll
-          for (int k = 0; k < MAXD; ++k) x[k] = (k < d) ? S.tab[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)] : 0.0;
-          double f = fn.template eval<MAXD>(S.desc, x);
+            for (int k = 1; k < MAXD; ++k)
+              if (k < d) f = __dmul_rn(f, S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)]);
+          } else {
+            double x[MAXD];
+#pragma unroll
+            for (int k = 0; k < MAXD; ++k)
+              x[k] = (k < d) ? S.tab[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)] : 0.0;
+            f = fn.template eval<MAXD>(S.desc, x);
+          }
           if (jac != 1.0) f = __dmul_rn(f, jac);
           if (base == 0) S.fv[p] = f;
           const double* w = &S.w[(int)(code >> 60) * kNRules];
@@ -407,9 +420,10 @@ static __global__ void __launch_bounds__(kRedThreads)
                          const double* __restrict__ left, const double* __restrict__ length, uint64_t stride,
                          const int32_t* __restrict__ bisect, const double* __restrict__ est,
                          double* __restrict__ out_left, double* __restrict__ out_length, uint64_t out_stride,
-                         uint32_t* __restrict__ out_owner, double* __restrict__ parent_out) {
+                         uint32_t* __restrict__ out_owner, double* __restrict__ parent_out, uint32_t chunk0) {
   __shared__ uint64_t sc[33];
-  const ChunkRef cr = chunks[blockIdx.x];
+  const uint32_t cidx = chunk0 + blockIdx.x;
+  const ChunkRef cr = chunks[cidx];
   const Transition T = trans[cr.integral];
   if (T.mode == 0) return;
   const SegDesc S = segs[cr.integral];
@@ -425,7 +439,7 @@ static __global__ void __launch_bounds__(kRedThreads)
   }
   uint64_t total;
   uint64_t pos = block_exclusive_scan(cnt, sc, &total);
-  pos += (T.mode == 2) ? (uint64_t)cr.local * kChunk : chunk_off[blockIdx.x];
+  pos += (T.mode == 2) ? (uint64_t)cr.local * kChunk : chunk_off[cidx];
 #pragma unroll
   for (int q = 0; q < kRedItems; ++q) {
     if (!keep[q]) continue;
@@ -452,8 +466,10 @@ static __global__ void __launch_bounds__(kRedThreads)
         }
       }
     }
-    out_owner[c0] = cr.integral;
-    out_owner[c1] = cr.integral;
+    if (out_owner) {
+      out_owner[c0] = cr.integral;
+      out_owner[c1] = cr.integral;
+    }
     parent_out[T.par_out + k] = est[i];
   }
 }
@@ -631,24 +647,25 @@ static __global__ void __launch_bounds__(kRedThreads) sum_final_kernel(const NS*
 
 namespace pg {
 
-// Initial uniform split of every integral of a batch (Sub_regions.cuh:11-36,
-// partition rule Workspace.cuh:379-387).  starts[j] is integral j's first
-// region, starts[njobs] the total.
-static __global__ void uniform_split_batch_kernel(double* __restrict__ left, double* __restrict__ length, uint64_t stride,
-                                           uint32_t* __restrict__ owner, const uint64_t* __restrict__ starts,
-                                           const IntegralDesc* __restrict__ descs, uint32_t njobs) {
-  const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= starts[njobs]) return;
-  uint32_t lo = 0, hi = njobs;  // largest j with starts[j] <= r
+// Initial uniform split of newly admitted integrals (Sub_regions.cuh:11-36,
+// partition rule Workspace.cuh:379-387).  Slot s covers regions
+// [starts[s], starts[s+1]) of the list and belongs to integral ids[s].
+static __global__ void uniform_split_batch_kernel(double* __restrict__ left, double* __restrict__ length,
+                                                  uint64_t stride, uint32_t* __restrict__ owner,
+                                                  const uint64_t* __restrict__ starts, const uint32_t* __restrict__ ids,
+                                                  const IntegralDesc* __restrict__ descs, uint32_t nslots) {
+  const uint64_t r = starts[0] + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= starts[nslots]) return;
+  uint32_t lo = 0, hi = nslots;  // largest s with starts[s] <= r
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) / 2;
     if (starts[mid] <= r) lo = mid; else hi = mid;
   }
-  const uint32_t j = lo;
+  const uint32_t j = ids[lo];
   const int d = descs[j].d;
   const int parts = d < 5 ? 4 : (d <= 10 ? 2 : 1);
   const double len = __ddiv_rn(1.0, (double)parts);
-  uint64_t q = r - starts[j];
+  uint64_t q = r - starts[lo];
   for (int k = 0; k < d; ++k) {
     const uint64_t id = q % (uint64_t)parts;
     q /= (uint64_t)parts;
@@ -656,6 +673,11 @@ static __global__ void uniform_split_batch_kernel(double* __restrict__ left, dou
     length[(uint64_t)k * stride + r] = len;
   }
   owner[r] = j;
+}
+
+static __global__ void fill_owner_kernel(uint32_t* __restrict__ owner, uint64_t start, uint64_t n, uint32_t j) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) owner[start + i] = j;
 }
 
 }  // namespace pg

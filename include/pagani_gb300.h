@@ -226,6 +226,18 @@ int pg_mcubes_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, d
 int pg_batch_integrate(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
                        const double* epsabs, const pg_options* opt, pg_result* out);
 
+/* Same as pg_batch_integrate; completion_ms[i] (may be NULL) receives the
+ * host time in milliseconds from the start of the call to the end of the
+ * iteration in which integral i finished (its latency within the batch). */
+int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
+                             const double* epsabs, const pg_options* opt, pg_result* out, double* completion_ms);
+
+/* Measurement utility, no counterpart in the reference: runs a fixed FP64
+ * fused-multiply-add loop on the context's GPU and returns the achieved
+ * FP64 rate in TFLOP/s (an FMA counts as 2 flops), the denominator of the
+ * region-evaluation roofline. */
+int pg_probe_fp64_peak(pg_context* ctx, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

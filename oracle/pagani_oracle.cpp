@@ -95,6 +95,25 @@ static inline double ipow(double s, int e) {
   return r;
 }
 
+// Per-axis factor of the product-form families.
+static double factor(const Prepared& p, int k, double x) {
+  switch (p.family) {
+    case FAM_PRODUCT_PEAK: {
+      const double t = x - p.u[k];
+      return 1.0 / std::fma(t, t, p.ia2[k]);
+    }
+    case FAM_GAUSSIAN: {
+      const double q = p.a[k] * (x - p.u[k]);
+      return std::exp(-(q * q));
+    }
+    case FAM_C0:
+      return std::exp(-(p.a[k] * std::fabs(x - p.u[k])));
+    case FAM_DISCONTINUOUS:
+      return (x > p.u[k]) ? 0.0 : std::exp(p.a[k] * x);
+  }
+  return 1.0;
+}
+
 static double eval(const Prepared& p, const double* x) {
   const int d = p.ndim;
   switch (p.family) {
@@ -105,39 +124,19 @@ static double eval(const Prepared& p, const double* x) {
       for (int i = 0; i < d; ++i) s = std::fma(p.a[i], x[i], s);
       return std::cos(s);
     }
-    case FAM_PRODUCT_PEAK: {
-      double v = 1.0;
-      for (int i = 0; i < d; ++i) {
-        const double t = x[i] - p.u[i];
-        const double term = 1.0 / std::fma(t, t, p.ia2[i]);
-        v = (i == 0) ? term : v * term;
-      }
+    case FAM_PRODUCT_PEAK:
+    case FAM_GAUSSIAN:
+    case FAM_C0:
+    case FAM_DISCONTINUOUS: {
+      // Product of per-axis factors, axis 0 first.
+      double v = factor(p, 0, x[0]);
+      for (int i = 1; i < d; ++i) v = v * factor(p, i, x[i]);
       return v;
     }
     case FAM_CORNER_PEAK: {
       double s = 1.0;
       for (int i = 0; i < d; ++i) s = std::fma(p.a[i], x[i], s);
       return 1.0 / ipow(s, d + 1);
-    }
-    case FAM_GAUSSIAN: {
-      double s = 0.0;
-      for (int i = 0; i < d; ++i) {
-        const double q = p.a[i] * (x[i] - p.u[i]);
-        s = std::fma(q, q, s);
-      }
-      return std::exp(-s);
-    }
-    case FAM_C0: {
-      double s = 0.0;
-      for (int i = 0; i < d; ++i) s = std::fma(p.a[i], std::fabs(x[i] - p.u[i]), s);
-      return std::exp(-s);
-    }
-    case FAM_DISCONTINUOUS: {
-      for (int i = 0; i < d; ++i)
-        if (x[i] > p.u[i]) return 0.0;
-      double s = 0.0;
-      for (int i = 0; i < d; ++i) s = std::fma(p.a[i], x[i], s);
-      return std::exp(s);
     }
     case FAM_PRODUCT: {
       double v = x[0];
