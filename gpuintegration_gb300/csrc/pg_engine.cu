@@ -133,7 +133,7 @@ Engine::Engine(int dev) : device(dev) {}
 
 Engine::~Engine() {
   cudaSetDevice(device);
-  DevBuf* dev_bufs[] = {&rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
+  DevBuf* dev_bufs[] = {&rule_trie_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
                         &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
                         &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
                         &thr_out_};
@@ -219,6 +219,13 @@ int Engine::init(std::string* why) {
     if (d == PG_MIN_NDIM) r2 = t;
   }
   code_coefficients(r2, R.A, R.B);
+  std::vector<uint16_t> tries;
+  for (int d = PG_MIN_NDIM; d <= kTrieMaxDim; ++d) {
+    RuleTable t = make_rule(d);
+    R.trie_off[d] = (int32_t)tries.size();
+    std::vector<uint16_t> tv = prefix_trie(t);
+    tries.insert(tries.end(), tv.begin(), tv.end());
+  }
   const double q = r2.G[1] / r2.G[0];
   R.ratio = q * q;
   if ((rc = ensure(rule_code_, codes.size() * 8)) != PG_OK) {
@@ -234,6 +241,12 @@ int Engine::init(std::string* why) {
   PG_INIT_TRY(cudaMemcpy(rule_w_.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice), "rule upload");
   PG_INIT_TRY(cudaMemcpy(rule_scale_.p, sc.data(), sc.size() * 8, cudaMemcpyHostToDevice), "rule upload");
   PG_INIT_TRY(cudaMemcpy(rule_norm_.p, nm.data(), nm.size() * 8, cudaMemcpyHostToDevice), "rule upload");
+  if ((rc = ensure(rule_trie_, tries.size() * 2)) != PG_OK) {
+    if (why) *why = last_error;
+    return rc;
+  }
+  PG_INIT_TRY(cudaMemcpy(rule_trie_.p, tries.data(), tries.size() * 2, cudaMemcpyHostToDevice), "rule upload");
+  R.trie = (const uint16_t*)rule_trie_.p;
   R.code = (const uint64_t*)rule_code_.p;
   R.w = (const double*)rule_w_.p;
   R.scale = (const double*)rule_scale_.p;

@@ -26,6 +26,8 @@ namespace pg {
 // Rule tables for every ndim, in device memory; passed by value.
 struct RuleDev {
   const uint64_t* code;             // packed points, concatenated over ndim
+  const uint16_t* trie;             // prefix tries (pg_rule.h), concatenated over ndim <= kTrieMaxDim
+  int32_t trie_off[kMaxNdim + 1];
   const double* w;                  // [(kMaxNdim + 1) * 45]
   const double* scale;
   const double* norm;
@@ -87,8 +89,22 @@ struct Transition {
 // tree per 32-lane half, then (half0 + 0) + half1.  Each per-axis coordinate
 // value a region can take (centre, +-G0..G4) is computed once per region.
 // ---------------------------------------------------------------------------
+// Trie buffers of the d <= 8 kernel: depth d-1 (at most feval(7) = 717 nodes)
+// and depth d-2 (at most feval(6) = 453), alternating downwards.
+constexpr int kTrieMaxDim = 8;
+constexpr int kTrieBufA = 720, kTrieBufB = 456;
+
+template <int MAXD>
+struct EvalTrieSmem {
+  double a[kTrieBufA];
+  double b[kTrieBufB];
+};
+template <>
+struct EvalTrieSmem<16> {};
+
 template <int MAXD>
 struct EvalWarpSmem {
+  EvalTrieSmem<MAXD> trie;
   IntegralDesc desc;
   double tab[MAXD * kCodesPerDim];
   double fac[MAXD * kCodesPerDim];  // per-axis factors of separable integrands
@@ -150,7 +166,34 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
     if (sep)
       for (int v = lane; v < d * kCodesPerDim; v += 32) S.fac[v] = fn.factor(S.desc, v / kCodesPerDim, S.tab[v]);
     __syncwarp();
+    // Product-form integrands with d <= 8: inner trie depths 2..d-1 (depth k
+    // goes to buffer a when d-1-k is even, else b; depth 1 is the axis-0
+    // factor row).  Depth d is formed point by point below.
+    const double* leaf_src = S.fac;
+    const uint16_t* leaf_tab = nullptr;
+    if constexpr (MAXD <= kTrieMaxDim) {
+      if (sep) {
+        const uint16_t* tt = rule.trie + rule.trie_off[d];
+        int off = 0;
+        for (int k = 2; k <= d - 1; ++k) {
+          const int m = rule.feval[k];
+          const double* src = (k - 1 == 1) ? S.fac : (((d - 1 - (k - 1)) & 1) ? S.trie.b : S.trie.a);
+          double* dst = ((d - 1 - k) & 1) ? S.trie.b : S.trie.a;
+          const double* fk = S.fac + (k - 1) * kCodesPerDim;
+          for (int i = lane; i < m; i += 32) {
+            const uint32_t e = __ldg(&tt[off + i]);
+            dst[i] = __dmul_rn(src[e & 0xfffu], fk[e >> 12]);
+          }
+          off += m;
+          __syncwarp();
+        }
+        leaf_src = (d == 2) ? S.fac : S.trie.a;
+        leaf_tab = tt + off;
+      }
+    }
+    const double* leaf_fac = S.fac + (d - 1) * kCodesPerDim;
     const double jac = S.desc.jac;
+    const bool scale = jac != 1.0;
     double sa0 = 0, sa1 = 0, sa2 = 0, sa3 = 0, sa4 = 0;
     double sb0 = 0, sb1 = 0, sb2 = 0, sb3 = 0, sb4 = 0;
     for (int base = 0; base < feval; base += 64) {
@@ -160,7 +203,10 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
         if (p < feval) {
           const uint64_t code = __ldg(&codes[p]);
           double f;
-          if (sep) {
+          if (sep && leaf_tab) {
+            const uint32_t e = __ldg(&leaf_tab[p]);
+            f = __dmul_rn(leaf_src[e & 0xfffu], leaf_fac[e >> 12]);
+          } else if (sep) {
             f = S.fac[(int)(code & 15u)];
 #pragma unroll
             for (int k = 1; k < MAXD; ++k)
@@ -172,7 +218,7 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
               x[k] = (k < d) ? S.tab[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)] : 0.0;
             f = fn.template eval<MAXD>(S.desc, x);
           }
-          if (jac != 1.0) f = __dmul_rn(f, jac);
+          if (scale) f = __dmul_rn(f, jac);
           if (base == 0) S.fv[p] = f;
           const double* w = &S.w[(int)(code >> 60) * kNRules];
           if (half == 0) {

@@ -198,6 +198,39 @@ RuleTable make_rule(int d) {
   return r;
 }
 
+std::vector<uint16_t> prefix_trie(const RuleTable& r) {
+  const int d = r.ndim;
+  std::vector<std::vector<uint8_t>> pts(r.feval, std::vector<uint8_t>(d));
+  for (int p = 0; p < r.feval; ++p)
+    for (int k = 0; k < d; ++k) pts[p][k] = (uint8_t)((r.code[p] >> (4 * k)) & 15u);
+  // levels[k]: node prefixes of depth k (k = 1..d)
+  std::vector<std::vector<std::vector<uint8_t>>> levels(d + 1);
+  std::vector<std::vector<uint16_t>> entries(d + 1);
+  levels[d] = pts;
+  for (int k = d; k >= 2; --k) {
+    std::vector<std::vector<uint8_t>>& up = levels[k - 1];
+    for (const auto& node : levels[k]) {
+      std::vector<uint8_t> pre(node.begin(), node.begin() + (k - 1));
+      int idx;
+      if (k - 1 == 1) {
+        idx = pre[0];
+      } else {
+        auto it = std::find(up.begin(), up.end(), pre);
+        if (it == up.end()) {
+          up.push_back(pre);
+          idx = (int)up.size() - 1;
+        } else {
+          idx = (int)(it - up.begin());
+        }
+      }
+      entries[k].push_back((uint16_t)(idx | ((int)node[k - 1] << 12)));
+    }
+  }
+  std::vector<uint16_t> out;
+  for (int k = 2; k <= d; ++k) out.insert(out.end(), entries[k].begin(), entries[k].end());
+  return out;
+}
+
 void code_coefficients(const RuleTable& r, double* A, double* B) {
   A[0] = .5 + 0.0;
   B[0] = .5 - 0.0;

@@ -32,6 +32,16 @@ struct RuleTable {
 int feval_count(int ndim);
 RuleTable make_rule(int ndim);
 
+// Prefix trie of the points' per-axis codes, for integrands that are a
+// left-to-right product of per-axis factors: a depth-k node is a distinct
+// prefix (c_0..c_{k-1}); its value is its parent's value times the factor of
+// axis k-1 at code c_{k-1}, so every point's product is formed with exactly
+// the roundings of v = f_0 * f_1 * ... * f_{d-1}, sharing common prefixes.
+// Depth-1 node i is code i.  Entries for depths 2..d follow each other; entry
+// = parent index (12 bits) | code << 12; depth d lists the points in rule
+// order.  Depth k has feval_count(k) nodes (feval_count(1) = 11).
+std::vector<uint16_t> prefix_trie(const RuleTable& r);
+
 // A = .5 + g and B = .5 - g for the 11 coordinate codes, as the reference
 // computes them per point (Sample.cuh:126-130).
 void code_coefficients(const RuleTable& r, double* A, double* B);
