@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpagani_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["pg_rule.cpp", "pg_engine.cu", "pg_capi.cu", "pg_mcubes.cu"]
+SOURCES = ["pg_rule.cpp", "pg_engine.cu", "pg_capi.cu", "pg_mcubes.cu", "pg_noalloc.cu"]
 
 
 def nvcc():

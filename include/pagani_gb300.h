@@ -238,6 +238,25 @@ int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand
  * region-evaluation roofline. */
 int pg_probe_fp64_peak(pg_context* ctx, double* tflops);
 
+/* Largest element count pg_reduce_sum_noalloc accepts (2^28 doubles). */
+#define PG_REDUCE_NOALLOC_MAX_N (1ull << 28)
+
+/* Compensated FP64 sum of the n doubles at d_x (device memory), written to
+ * *d_out (device memory), asynchronously on `stream` (a cudaStream_t of the
+ * current device; NULL for the default stream).  No counterpart in the
+ * reference: it is the allocation-free form of pg_reduce_sum, for callers that
+ * cannot allocate device memory -- a program whose device memory is owned by
+ * another allocator, or a loop that cannot take cudaMalloc's implicit
+ * synchronisation.  It calls no allocator; its only scratch is a fixed 2 MB
+ * array in the library's device image, which every GPU that loads the
+ * library holds until the process exits.  n above PG_REDUCE_NOALLOC_MAX_N is
+ * rejected with PG_BAD_ARG before anything runs.  The first call on a device
+ * looks up that array's device address, so make it before any stream capture.
+ * Every call uses the same array: calls whose kernels can overlap on the GPU
+ * (other streams, other host threads) race, and the caller must serialise
+ * them.  The result is bit-identical to pg_reduce_sum on the same data. */
+int pg_reduce_sum_noalloc(const double* d_x, uint64_t n, double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
