@@ -72,7 +72,8 @@ __device__ __forceinline__ double family_factor(const IntegralDesc& D, int k, do
     }
     case FAM_GAUSSIAN: {
       const double q = __dmul_rn(D.a[k], __dsub_rn(x, D.u[k]));
-      return exp(-__dmul_rn(q, q));
+      const double v = exp(-__dmul_rn(q, q));
+      return D.c != 0.0 ? __dmul_rn(v, D.c) : v;  // c: per-axis normalisation (0 = none)
     }
     case FAM_C0:
       return exp(-__dmul_rn(D.a[k], fabs(__dsub_rn(x, D.u[k]))));

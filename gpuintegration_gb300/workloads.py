@@ -56,7 +56,9 @@ def analytic(f: Integrand) -> float:
             total += (-1 if bin(mask).count("1") % 2 else 1) / s
         return float(total / (math.factorial(d) * math.prod(fa)))
     if f.family == GAUSSIAN:
-        return math.prod(math.sqrt(math.pi) / (2 * ai) * (_erf(ai * (1 - ui)) + _erf(ai * ui)) for ai, ui in zip(a, u))
+        scale = float(f.c) if f.c else 1.0
+        return math.prod(scale * math.sqrt(math.pi) / (2 * ai) * (_erf(ai * (1 - ui)) + _erf(ai * ui))
+                         for ai, ui in zip(a, u))
     if f.family == C0:
         return math.prod((2 - math.exp(-ai * ui) - math.exp(-ai * (1 - ui))) / ai for ai, ui in zip(a, u))
     if f.family == DISCONTINUOUS:
@@ -157,3 +159,9 @@ def config5_cases(count: int, master: int = 5000) -> List[Case]:
 
 def within_tolerance(estimate: float, exact: float, epsrel: float) -> bool:
     return abs(estimate - exact) <= epsrel * abs(exact)
+
+
+def config3_integrand(sigma: float = 0.01, d: int = 6) -> Integrand:
+    """m-Cubes configuration: exp(-sum (x_i - 0.5)^2 / (2 sigma^2)) / (sigma sqrt(2 pi))^d on [0,1]^d."""
+    a = 1.0 / (sigma * math.sqrt(2.0))
+    return Integrand(GAUSSIAN, d, [a] * d, [0.5] * d, c=1.0 / (sigma * math.sqrt(2.0 * math.pi)))

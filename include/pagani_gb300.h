@@ -46,7 +46,7 @@ typedef enum pg_status {
  *   OSCILLATORY     cos(2*pi*u_0 + sum a_i x_i)
  *   PRODUCT_PEAK    prod 1 / (a_i^-2 + (x_i - u_i)^2)
  *   CORNER_PEAK     (1 + sum a_i x_i)^-(d+1)
- *   GAUSSIAN        exp(-sum a_i^2 (x_i - u_i)^2)
+ *   GAUSSIAN        exp(-sum a_i^2 (x_i - u_i)^2), times c^d when c != 0 (normalised Gaussians)
  *   C0              exp(-sum a_i |x_i - u_i|)
  *   DISCONTINUOUS   0 if any x_i > u_i, else exp(sum a_i x_i)
  * and the test integrands of the reference's own tests:

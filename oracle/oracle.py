@@ -12,7 +12,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "build")
 LIB = os.path.join(BUILD, "liboracle.so")
-SOURCES = ["pagani_oracle.cpp", "mcubes_oracle.cpp"]
+SOURCES = ["pagani_oracle.cpp"]
 
 _lib = None
 _D = ctypes.POINTER(ctypes.c_double)
@@ -59,6 +59,7 @@ def load():
     lib.orc_integrate.restype = ctypes.c_int
     lib.orc_integrate.argtypes = [vp, ctypes.c_double, ctypes.c_double, _D, _D, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, ctypes.c_int, P(OrcResult), _D, ctypes.c_int]
+    lib.orc_philox.argtypes = [P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_uint32)]
     if hasattr(lib, "orc_mcubes_integrate"):
         lib.orc_mcubes_integrate.restype = ctypes.c_int
         lib.orc_mcubes_integrate.argtypes = [vp, ctypes.c_double, ctypes.c_double, _D, _D, ctypes.c_double,
@@ -165,5 +166,29 @@ def integrate(f, epsrel, epsabs, lows=None, highs=None, relerr_classification=Tr
     s = _integrand_struct(f)
     nt = lib.orc_integrate(ctypes.byref(s), epsrel, epsabs, _p(lows), _p(highs), 1 if relerr_classification else 0,
                            device_mem, max_iters, nthreads or os.cpu_count() or 1, ctypes.byref(r), _p(tr), trace_cap)
+    assert nt >= 0, nt
+    return r, tr[:nt]
+
+
+def philox(ctr, key):
+    lib = load()
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib.orc_philox(c, k, o)
+    return list(o)
+
+
+def mcubes_integrate(f, epsrel, epsabs, ncall, titer=15, itmax=15, skip=5, nbins=500, seed=0x5EED, alpha=1.5,
+                     lows=None, highs=None, trace_cap=0):
+    lib = load()
+    d = f.ndim
+    lows = np.zeros(d) if lows is None else np.ascontiguousarray(lows, dtype=np.float64)
+    highs = np.ones(d) if highs is None else np.ascontiguousarray(highs, dtype=np.float64)
+    r = OrcResult()
+    tr = np.zeros((max(trace_cap, 1), 4))
+    s = _integrand_struct(f)
+    nt = lib.orc_mcubes_integrate(ctypes.byref(s), epsrel, epsabs, _p(lows), _p(highs), ncall, titer, itmax, skip,
+                                  nbins, seed, alpha, ctypes.byref(r), _p(tr), trace_cap)
     assert nt >= 0, nt
     return r, tr[:nt]

@@ -104,7 +104,8 @@ static double factor(const Prepared& p, int k, double x) {
     }
     case FAM_GAUSSIAN: {
       const double q = p.a[k] * (x - p.u[k]);
-      return std::exp(-(q * q));
+      const double v = std::exp(-(q * q));
+      return p.c != 0.0 ? v * p.c : v;
     }
     case FAM_C0:
       return std::exp(-(p.a[k] * std::fabs(x - p.u[k])));
@@ -943,6 +944,283 @@ int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const d
   cum.nregions += n;
   *out = cum;
   return ntrace;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// m-Cubes oracle.  Restates cuda_mcubes::vegas (cuda/mcubes/vegasT.cuh:643-997)
+// and its sampling kernel (vegasT.cuh:136-485) with the library's random
+// stream (Philox4x32-10, counter = cube, sample, axis pair, iteration) and
+// its work split (1024 x 256 threads, contiguous cube runs, per-thread sums,
+// 32-lane shuffle-down trees then 8 warp sums in order), so the estimate and
+// its variance match the GPU's up to the order of the f^2 bin sums.
+// ===========================================================================
+namespace orc {
+
+static void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  // Philox4x32-10, Salmon, Moraes, Dror, Shaw, SC'11.
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[1] = (uint32_t)p1;
+    c[3] = (uint32_t)p0;
+    c[0] = n0;
+    c[2] = n2;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+static double unit53(uint32_t a, uint32_t b) {
+  const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+  return (double)(m + 1) * 1.1102230246251565404236316680908203125e-16;
+}
+
+static void mc_rebin(double rc, int nd, const double* r, double* xin, double* xi) {
+  int k = 0;
+  double dr = 0.0, xn = 0.0, xo = 0.0;
+  for (int i = 1; i < nd; i++) {
+    while (rc > dr) dr += r[++k];
+    if (k > 1) xo = xi[k - 1];
+    xn = xi[k];
+    dr -= rc;
+    xin[i] = xn - (xn - xo) * dr / r[k];
+  }
+  for (int i = 1; i < nd; i++) xi[i] = xin[i];
+  xi[nd] = 1.0;
+}
+
+}  // namespace orc
+
+extern "C" {
+
+void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  orc::philox(c, key[0], key[1]);
+  for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
+
+int orc_mcubes_integrate(const orc::Integrand* f, double epsrel, double epsabs, const double* lows,
+                         const double* highs, double ncall, int titer, int itmax, int skip, int nbins, uint64_t seed,
+                         double alpha, orc_result* out, double* trace, int trace_cap) {
+  using namespace orc;
+  const int d = f->ndim;
+  const Prepared P = prepare(*f);
+  const int nd = nbins > 1 ? nbins : 500;
+  const int nb1 = nd + 1;
+  const uint64_t ng = (uint64_t)std::pow(ncall / 2.0 + 0.25, 1.0 / d);
+  if (ng < 1) return -1;
+  double k = 1;
+  for (int i = 1; i < d; ++i) k *= (double)ng;
+  k *= (double)ng;
+  const uint64_t ncubes = (uint64_t)k;
+  const int npg = (int)std::max(ncall / k, 2.0);
+  const double calls = (double)npg * k;
+  double dxg = 1.0 / (double)ng, dv2g = 1;
+  for (int i = 1; i <= d; ++i) dv2g *= dxg;
+  dv2g = (calls * dv2g * calls * dv2g) / npg / npg / (npg - 1.0);
+  const double xnd = nd;
+  dxg *= xnd;
+  double xjac = 1.0 / calls;
+  std::vector<double> regn(d), dx(d);
+  for (int j = 0; j < d; ++j) {
+    regn[j] = lows ? lows[j] : 0.0;
+    dx[j] = (highs ? highs[j] : 1.0) - regn[j];
+    xjac *= dx[j];
+  }
+  std::vector<double> xi((size_t)d * nb1, 0.0), r(nb1, 1.0), xin(nb1, 0.0), dbin((size_t)d * nb1), dt(d);
+  for (int j = 0; j < d; ++j) {
+    xi[(size_t)j * nb1 + 1] = 1.0;
+    mc_rebin(1.0 / xnd, nd, r.data(), xin.data(), &xi[(size_t)j * nb1]);
+  }
+  const int NB = 1024, NT = 256;
+  const uint64_t nthreads = (uint64_t)NB * NT, per = (ncubes + nthreads - 1) / nthreads;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  std::vector<double> part(2 * NB);
+  const int nworkers = std::max(1u, std::thread::hardware_concurrency());
+  auto iteration = [&](int it, bool adapt) {
+    std::fill(dbin.begin(), dbin.end(), 0.0);
+    std::vector<std::vector<double>> wbins(nworkers, std::vector<double>(adapt ? dbin.size() : 0, 0.0));
+    std::vector<std::thread> th;
+    for (int w = 0; w < nworkers; ++w) {
+      th.emplace_back([&, w] {
+        std::vector<double>& hb = wbins[w];
+        for (int b = w; b < NB; b += nworkers) {
+          double lane_fb[NT], lane_f2b[NT];
+          for (int t = 0; t < NT; ++t) {
+            const uint64_t tid = (uint64_t)b * NT + t;
+            const uint64_t c0 = tid * per, c1 = std::min(ncubes, c0 + per);
+            double fbg = 0.0, f2bg = 0.0;
+            for (uint64_t cube = c0; cube < c1; ++cube) {
+              int kg[kMaxDim];
+              uint64_t q = cube;
+              for (int j = d - 1; j >= 0; --j) {
+                kg[j] = 1 + (int)(q % ng);
+                q /= ng;
+              }
+              double fb = 0.0, f2b = 0.0;
+              for (int s = 1; s <= npg; ++s) {
+                double wgt = xjac, x[kMaxDim];
+                int ia[kMaxDim];
+                uint32_t rnd[4] = {0, 0, 0, 0};
+                for (int j = 0; j < d; ++j) {
+                  if ((j & 1) == 0) {
+                    rnd[0] = (uint32_t)cube;
+                    rnd[1] = (uint32_t)s | ((uint32_t)(cube >> 32) << 16);
+                    rnd[2] = (uint32_t)(j >> 1);
+                    rnd[3] = (uint32_t)it;
+                    philox(rnd, k0, k1);
+                  }
+                  const double ran = (j & 1) ? unit53(rnd[2], rnd[3]) : unit53(rnd[0], rnd[1]);
+                  const double xn = std::fma((double)kg[j] - ran, dxg, 1.0);
+                  const int bb = std::max(std::min((int)xn, nd), 1);
+                  const double* xij = &xi[(size_t)j * nb1];
+                  double xo, rc;
+                  if (bb > 1) {
+                    xo = xij[bb] - xij[bb - 1];
+                    rc = std::fma(xn - (double)bb, xo, xij[bb - 1]);
+                  } else {
+                    xo = xij[bb];
+                    rc = (xn - (double)bb) * xo;
+                  }
+                  x[j] = std::fma(rc, dx[j], regn[j]);
+                  wgt = wgt * (xo * xnd);
+                  ia[j] = bb;
+                }
+                const double fv = wgt * eval(P, x);
+                const double f2 = fv * fv;
+                fb = fb + fv;
+                f2b = f2b + f2;
+                if (adapt)
+                  for (int j = 0; j < d; ++j) hb[(size_t)j * nb1 + ia[j]] += f2;
+              }
+              f2b = std::sqrt(f2b * (double)npg);
+              f2b = (f2b - fb) * (f2b + fb);
+              if (f2b <= 0.0) f2b = 1.0e-30;
+              fbg = fbg + fb;
+              f2bg = f2bg + f2b;
+            }
+            lane_fb[t] = fbg;
+            lane_f2b[t] = f2bg;
+          }
+          double w0[8], w1[8];
+          for (int w8 = 0; w8 < 8; ++w8) {
+            double a[32], c[32];
+            for (int l = 0; l < 32; ++l) {
+              a[l] = lane_fb[w8 * 32 + l];
+              c[l] = lane_f2b[w8 * 32 + l];
+            }
+            for (int off = 16; off >= 1; off >>= 1)
+              for (int l = 0; l < off; ++l) {
+                a[l] = a[l] + a[l + off];
+                c[l] = c[l] + c[l + off];
+              }
+            w0[w8] = a[0];
+            w1[w8] = c[0];
+          }
+          double s0 = 0.0, s1 = 0.0;
+          for (int w8 = 0; w8 < 8; ++w8) {
+            s0 = s0 + w0[w8];
+            s1 = s1 + w1[w8];
+          }
+          part[2 * b] = s0;
+          part[2 * b + 1] = s1;
+        }
+      });
+    }
+    for (auto& t : th) t.join();
+    if (adapt)
+      for (int w = 0; w < nworkers; ++w)
+        for (size_t i = 0; i < dbin.size(); ++i) dbin[i] += wbins[w][i];
+    double ti = 0, tsi = 0;
+    for (int b = 0; b < NB; ++b) {
+      ti += part[2 * b];
+      tsi += part[2 * b + 1];
+    }
+    return std::make_pair(ti, tsi * dv2g);
+  };
+  double si = 0, swgt = 0, schi = 0, tgral = 0, sd = 0, chi2a = 0;
+  int status = 1, ntr = 0;
+  uint64_t iters = 0;
+  auto record = [&](int it, double ti, double tsi) {
+    if (trace && ntr < trace_cap) {
+      double* t = trace + 4 * ntr++;
+      t[0] = it;
+      t[1] = ti;
+      t[2] = tsi;
+      t[3] = tgral;
+    }
+  };
+  for (int it = 1; it <= itmax && status == 1; ++iters, ++it) {
+    auto [ti, tsi] = iteration(it, true);
+    if (it > skip) {
+      const double wgt = 1.0 / tsi;
+      si += wgt * ti;
+      schi += wgt * ti * ti;
+      swgt += wgt;
+      tgral = si / swgt;
+      chi2a = (schi - si * tgral) / (static_cast<double>(it) - 0.9999);
+      if (chi2a < 0.0) chi2a = 0.0;
+      sd = std::sqrt(1.0 / swgt);
+      const bool ok = std::fabs(sd / tgral) <= epsrel || sd <= epsabs;
+      status = (ok && it >= 5) ? 0 : 1;
+    }
+    record(it, ti, tsi);
+    for (int j = 0; j < d; ++j) {
+      double* dj = &dbin[(size_t)j * nb1];
+      double xo = dj[1], xn = dj[2];
+      dj[1] = (xo + xn) / 2.0;
+      dt[j] = dj[1];
+      for (int i = 2; i < nd; ++i) {
+        const double rcv = xo + xn;
+        xo = xn;
+        xn = dj[i + 1];
+        dj[i] = (rcv + xn) / 3.0;
+        dt[j] += dj[i];
+      }
+      dj[nd] = (xo + xn) / 2.0;
+      dt[j] += dj[nd];
+    }
+    for (int j = 0; j < d; ++j) {
+      if (dt[j] > 0.0) {
+        const double* dj = &dbin[(size_t)j * nb1];
+        double rsum = 0.0;
+        for (int i = 1; i <= nd; ++i) {
+          r[i] = std::pow((1.0 - dj[i] / dt[j]) / (std::log(dt[j]) - std::log(dj[i])), alpha);
+          rsum += r[i];
+        }
+        mc_rebin(rsum / xnd, nd, r.data(), xin.data(), &xi[(size_t)j * nb1]);
+      }
+    }
+  }
+  for (int it = itmax + 1; it <= titer && status; ++iters, ++it) {
+    auto [ti, tsi] = iteration(it, false);
+    const double wgt = 1.0 / tsi;
+    si += wgt * ti;
+    schi += wgt * ti * ti;
+    swgt += wgt;
+    tgral = si / swgt;
+    chi2a = (schi - si * tgral) / (it - 0.9999);
+    if (chi2a < 0.0) chi2a = 0.0;
+    sd = std::sqrt(1.0 / swgt);
+    const bool ok = std::fabs(sd / tgral) <= epsrel || sd <= epsabs;
+    status = (ok && it >= 5) ? 0 : 1;
+    record(it, ti, tsi);
+  }
+  orc_result R{};
+  R.estimate = tgral;
+  R.errorest = sd;
+  R.chi_sq = chi2a;
+  R.neval = (uint64_t)calls * iters;
+  R.nregions = ncubes;
+  R.iters = iters;
+  R.status = status;
+  R.last_phase = -1;
+  *out = R;
+  return ntr;
 }
 
 }  // extern "C"
