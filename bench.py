@@ -47,7 +47,70 @@ def parse():
     p.add_argument("--plain-sample", type=int, default=512)
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--max-regions", type=int, default=1 << 26)
+    p.add_argument("--config", type=int, default=4, choices=[3, 4, 5],
+                   help="4: batched workload (default, the metric's configuration); 5: served workload; "
+                        "3: m-Cubes Gaussian")
+    p.add_argument("--rate", type=float, default=2000.0, help="config 5: Poisson arrival rate (requests/s)")
+    p.add_argument("--duration", type=float, default=60.0, help="config 5: arrival window (s)")
+    p.add_argument("--budget-gb", type=float, default=120.0, help="config 5: device budget of the region pool")
+    p.add_argument("--serve-seconds", type=float, default=0.0,
+                   help="config 5: stop serving after this many seconds (0: arrival window + 60 s)")
     return p.parse_args()
+
+
+def run_served(args):
+    """Served PAGANI (Poisson arrivals, continuous batching, HBM budget)."""
+    import gpuintegration_gb300 as pg
+    from gpuintegration_gb300 import workloads as W
+    arrivals = W.poisson_arrivals(args.rate, args.duration)
+    cases = W.config5_cases(len(arrivals))
+    ctx = pg.Context(0)
+    fs = (pg.PgIntegrand * len(cases))(*[c.integrand.to_c() for c in cases])
+    eps = np.array([c.epsrel for c in cases])
+    clocks = ClockSampler(0)
+    clocks.start()
+    deadline = 1000.0 * (args.serve_seconds if args.serve_seconds > 0 else args.duration + 60.0)
+    t0 = time.perf_counter()
+    res, done = ctx.serve(fs, eps, 0.0, arrivals, budget_bytes=int(args.budget_gb * 1e9), deadline_ms=deadline)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    fin = done >= 0
+    lat = (done - arrivals)[fin]
+    arrived = int((arrivals <= wall * 1000.0).sum())
+    conv = sum(1 for c, r, ok in zip(cases, res, fin) if ok and within(c, r))
+    st = ctx.stats()
+    line = {"metric": "served PAGANI: integrals/s and p50/p99 latency", "value": conv / wall, "unit": "integrals/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"Poisson arrivals {args.rate:g}/s for {args.duration:g} s, Genz dim 3..10, "
+                                   f"epsrel log-U[1e-6,1e-3]", "requests": len(cases), "budget_gb": args.budget_gb,
+                       "deadline_s": deadline / 1000.0},
+            "latency_ms_finished": {"p50": float(np.percentile(lat, 50)) if lat.size else None,
+                                    "p99": float(np.percentile(lat, 99)) if lat.size else None,
+                                    "max": float(lat.max()) if lat.size else None},
+            "arrived": arrived, "finished": int(fin.sum()), "unfinished_at_deadline": int((~fin).sum()),
+            "wall_s": wall, "converged_within_tolerance": conv,
+            "status0": sum(1 for r, ok in zip(res, fin) if ok and r.status == 0),
+            "gpu_launches": int(st.launches), "points_per_s": st.points_evaluated / wall, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_mcubes(args):
+    """m-Cubes on the 6-D sigma = 0.01 Gaussian (2^24 calls x 20 iterations, fixed seed)."""
+    import gpuintegration_gb300 as pg
+    from gpuintegration_gb300 import workloads as W
+    ctx = pg.Context(0)
+    f = W.config3_integrand()
+    for _ in range(args.warmup):
+        ctx.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 24, titer=20, itmax=20, skip=5, seed=2024)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = ctx.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 24, titer=20, itmax=20, skip=5, seed=2024)
+    el = (time.perf_counter() - t0) / args.steps
+    line = {"metric": "m-Cubes time to solution, 6-D Gaussian sigma 0.01", "value": el * 1000, "unit": "ms",
+            "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "estimate": r.estimate, "errorest": r.errorest, "sigma_from_1": (r.estimate - 1.0) / r.errorest,
+            "iters": r.iters, "status": r.status, "samples_per_s": r.neval / el}
+    print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -202,6 +265,10 @@ def run_reference(args, cases, rank, world):
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
+    if args.config == 5 and args.impl == "gb300":
+        return run_served(args)
+    if args.config == 3 and args.impl == "gb300":
+        return run_mcubes(args)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -131,6 +131,8 @@ def load_library(path: str = LIB_PATH):
         "pg_batch_integrate_timed": (ctypes.c_int, [c_ctx, ctypes.c_uint64, P(PgIntegrand), _D, _D, P(PgOptions),
                                                     P(PgResult), _D]),
         "pg_probe_fp64_peak": (ctypes.c_int, [c_ctx, _D]),
+        "pg_serve": (ctypes.c_int, [c_ctx, ctypes.c_uint64, P(PgIntegrand), _D, _D, _D, ctypes.c_uint64,
+                                    ctypes.c_double, P(PgOptions), P(PgResult), _D]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -292,6 +294,21 @@ class Context:
         self._check(self.lib.pg_batch_integrate_timed(self.h, n, arr, _ptr(er), _ptr(ea), ctypes.byref(o), out,
                                                       _ptr(completion_ms)))
         return [IntegrationResult.from_c(out[i]) for i in range(n)]
+
+    def serve(self, fs, epsrel, epsabs, arrival_ms, budget_bytes: int = 0, options: Optional[PgOptions] = None,
+              deadline_ms: float = 0.0):
+        """Continuous-batching run over an arrival schedule; returns (results, completion_ms)."""
+        n = len(fs)
+        arr = fs if isinstance(fs, ctypes.Array) else (PgIntegrand * n)(*[f.to_c() for f in fs])
+        er = np.ascontiguousarray(np.broadcast_to(np.asarray(epsrel, dtype=np.float64), (n,)))
+        ea = np.ascontiguousarray(np.broadcast_to(np.asarray(epsabs, dtype=np.float64), (n,)))
+        arrival = np.ascontiguousarray(arrival_ms, dtype=np.float64)
+        done = np.zeros(n)
+        out = (PgResult * n)()
+        o = options if options is not None else default_options()
+        self._check(self.lib.pg_serve(self.h, n, arr, _ptr(er), _ptr(ea), _ptr(arrival), int(budget_bytes),
+                                      float(deadline_ms), ctypes.byref(o), out, _ptr(done)))
+        return [IntegrationResult.from_c(out[i]) for i in range(n)], done
 
     def probe_fp64_peak(self) -> float:
         """Measured FP64 FMA rate of this GPU in TFLOP/s."""

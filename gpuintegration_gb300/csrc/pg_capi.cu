@@ -261,6 +261,41 @@ int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand
   return PG_OK;
 }
 
+int pg_serve(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel, const double* epsabs,
+             const double* arrival_ms, uint64_t budget_bytes, double deadline_ms, const pg_options* opt,
+             pg_result* out, double* completion_ms) {
+  if (!ctx || (count && (!fs || !epsrel || !epsabs || !arrival_ms || !out)))
+    return set_err(ctx, PG_BAD_ARG, "null argument");
+  if (count > 0xffffffffull) return set_err(ctx, PG_BAD_ARG, "too many requests");
+  for (uint64_t i = 1; i < count; ++i)
+    if (arrival_ms[i] < arrival_ms[i - 1]) return set_err(ctx, PG_BAD_ARG, "arrivals must be ascending");
+  Guard g(ctx);
+  std::vector<pg::Job> jobs(count);
+  for (uint64_t i = 0; i < count; ++i) {
+    std::string why;
+    int rc = validate_eps(ctx, epsrel[i], epsabs[i]);
+    if (rc != PG_OK) return rc;
+    rc = pg::prepare_desc(fs[i], nullptr, nullptr, &jobs[i].desc, &why);
+    if (rc != PG_OK) return set_err(ctx, rc, "request " + std::to_string(i) + ": " + why);
+    jobs[i].epsrel = epsrel[i];
+    jobs[i].epsabs = epsabs[i];
+    if (opt) jobs[i].opt = *opt; else pg_options_default(&jobs[i].opt);
+    if (jobs[i].opt.max_iters <= 0) jobs[i].opt.max_iters = 700;
+  }
+  pg::RunPolicy pol;
+  pol.arrival_ms = arrival_ms;
+  pol.budget_bytes = budget_bytes;
+  pol.deadline_ms = deadline_ms;
+  if (opt) pol.max_regions = opt->max_regions;
+  int rc = ctx->eng->run(jobs, pg::launch_family_eval, pol);
+  if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
+  for (uint64_t i = 0; i < count; ++i) {
+    out[i] = jobs[i].res;
+    if (completion_ms) completion_ms[i] = jobs[i].done_ms;
+  }
+  return PG_OK;
+}
+
 int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,
                                uint64_t n, const double* d_left, const double* d_length, double* d_est, double* d_err,
                                int32_t* d_bisect, int32_t eval_mode) {

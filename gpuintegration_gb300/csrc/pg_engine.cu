@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <sstream>
@@ -485,6 +486,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     PG_TRY(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
     cap = (uint64_t)(0.6 * (double)fr) / bytes_per_region;
   }
+  if (policy.budget_bytes) cap = std::min<uint64_t>(cap, policy.budget_bytes / bytes_per_region);
   cap = std::max<uint64_t>(cap, 4096);
   const uint64_t admit_limit = (uint64_t)(policy.admit_fraction * (double)cap);
   // Per-integral arrays.
@@ -539,9 +541,22 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   std::vector<int> mode(njobs);
   std::vector<uint64_t> keepA(njobs);
   std::vector<uint32_t> adm_pending;
+  auto elapsed_ms = [&]() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  };
   while (true) {
+    if (policy.deadline_ms > 0 && elapsed_ms() > policy.deadline_ms) {
+      for (uint32_t j = 0; j < njobs; ++j)
+        if (jobs[j].state != JOB_DONE) {
+          jobs[j].res.status = -1;  // not finished before the deadline
+          jobs[j].done_ms = -1.0;
+          jobs[j].state = JOB_DONE;
+        }
+      break;
+    }
     // ---- admission: waiting integrals join at the end of the list, in order
     adm_pending.clear();
+    const double now_admit = elapsed_ms();
     {
       uint64_t t = T, pp = P;
       uint64_t* hs = (uint64_t*)h_adm_starts_.p;
@@ -551,6 +566,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       for (uint32_t j = first_waiting; j < njobs; ++j) {
         Job& J = jobs[j];
         if (J.state != JOB_PENDING && J.state != JOB_SPILLED) continue;
+        if (J.state == JOB_PENDING && policy.arrival_ms && policy.arrival_ms[j] > now_admit) break;  // not yet arrived
         if (t + J.n > admit_limit && t > 0) break;
         J.start = t;
         J.par_start = pp;
@@ -605,7 +621,22 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     live.clear();
     for (uint32_t j = 0; j < njobs; ++j)
       if (jobs[j].state == JOB_RESIDENT) live.push_back(j);
-    if (live.empty()) break;
+    if (live.empty()) {
+      // Idle: wait for the next arrival, or stop when every job is done.
+      uint32_t next = njobs;
+      for (uint32_t j = first_waiting; j < njobs; ++j)
+        if (jobs[j].state == JOB_PENDING || jobs[j].state == JOB_SPILLED) {
+          next = j;
+          break;
+        }
+      if (next == njobs) break;
+      if (policy.arrival_ms && jobs[next].state == JOB_PENDING) {
+        double wait = policy.arrival_ms[next] - elapsed_ms();
+        if (policy.deadline_ms > 0) wait = std::min(wait, policy.deadline_ms - elapsed_ms() + 0.001);
+        if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double, std::milli>(wait));
+      }
+      continue;
+    }
     // Segments and chunk list of the resident integrals.
     chunk_list.clear();
     SegDesc* hs = (SegDesc*)h_segs_.p;

@@ -89,6 +89,13 @@ struct Job {
 struct RunPolicy {
   uint64_t max_regions = 0;   // pool capacity in regions (0: from free device memory)
   double admit_fraction = 0.5;  // new work is admitted while the list is below this share of the pool
+  uint64_t budget_bytes = 0;  // device bytes the pool may use (0: no byte budget); caps max_regions
+  // Serving: job j may not be admitted before arrival_ms[j] (ascending), in
+  // milliseconds from the start of the run; nullptr admits every job at once.
+  const double* arrival_ms = nullptr;
+  // Serving: stop at the first iteration boundary after this many milliseconds
+  // (0: run to completion); unfinished jobs keep status -1 and done_ms -1.
+  double deadline_ms = 0;
 };
 
 // Prepares an IntegralDesc from the C ABI description (host, no contraction).

@@ -45,6 +45,13 @@ def analytic(f: Integrand) -> float:
         return z.real
     if f.family == PRODUCT_PEAK:
         return math.prod(ai * (math.atan(ai * (1 - ui)) + math.atan(ai * ui)) for ai, ui in zip(a, u))
+    if f.family == CORNER_PEAK and d > 8:
+        # alternating sum over the 2^d vertices, summed exactly (math.fsum) from rounded terms
+        terms = []
+        for mask in range(1 << d):
+            s = math.fsum(a[k] for k in range(d) if mask >> k & 1)
+            terms.append((-1.0 if bin(mask).count("1") % 2 else 1.0) / (1.0 + s))
+        return math.fsum(terms) / (math.factorial(d) * math.prod(a))
     if f.family == CORNER_PEAK:
         fa = [Fraction(x) for x in a]
         total = Fraction(0)
@@ -165,3 +172,11 @@ def config3_integrand(sigma: float = 0.01, d: int = 6) -> Integrand:
     """m-Cubes configuration: exp(-sum (x_i - 0.5)^2 / (2 sigma^2)) / (sigma sqrt(2 pi))^d on [0,1]^d."""
     a = 1.0 / (sigma * math.sqrt(2.0))
     return Integrand(GAUSSIAN, d, [a] * d, [0.5] * d, c=1.0 / (sigma * math.sqrt(2.0 * math.pi)))
+
+
+def poisson_arrivals(rate_per_s: float, duration_s: float, seed: int = 5005) -> "np.ndarray":
+    """Arrival times in milliseconds of a Poisson process, ascending."""
+    rng = np.random.default_rng(seed)
+    n = int(rate_per_s * duration_s * 1.2) + 16
+    t = np.cumsum(rng.exponential(1000.0 / rate_per_s, size=n))
+    return t[t < duration_s * 1000.0]

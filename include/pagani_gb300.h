@@ -232,6 +232,26 @@ int pg_batch_integrate(pg_context* ctx, uint64_t count, const pg_integrand* fs, 
 int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
                              const double* epsabs, const pg_options* opt, pg_result* out, double* completion_ms);
 
+/* ---------------- served PAGANI ----------------
+ * Continuous batching over an arrival schedule: request i (integrand fs[i],
+ * tolerances epsrel[i]/epsabs[i]) arrives arrival_ms[i] milliseconds after the
+ * call starts (ascending).  At every iteration boundary the requests that have
+ * arrived join the device region pool, in arrival order, while the pool's
+ * footprint stays under budget_bytes of device memory (0: 60% of free memory);
+ * their regions are evaluated in the same launches as the requests already
+ * running, each request's region list stays on the device across iterations
+ * (or moves to host memory while the pool is full), and each request retires
+ * in the iteration it converges.  completion_ms[i] receives the time the
+ * result was ready (latency = completion_ms[i] - arrival_ms[i]).  With
+ * deadline_ms > 0 the call returns at the first iteration boundary after that
+ * time; requests not finished by then get status -1 and completion_ms -1.
+ * Every finished result is bit-identical to pg_integrate's for the same
+ * request.  No counterpart in the reference (a loop of Workspace::integrate
+ * calls, Workspace.cuh:361-494). */
+int pg_serve(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel, const double* epsabs,
+             const double* arrival_ms, uint64_t budget_bytes, double deadline_ms, const pg_options* opt,
+             pg_result* out, double* completion_ms);
+
 /* Measurement utility, no counterpart in the reference: runs a fixed FP64
  * fused-multiply-add loop on the context's GPU and returns the achieved
  * FP64 rate in TFLOP/s (an FMA counts as 2 flops), the denominator of the
