@@ -261,12 +261,18 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
 
     // Split axis from the fourth differences (Sample.cuh:194-218): the first
     // axis whose difference is the largest, if positive; else the widest axis.
+    // base + ratio*(fp+fm) - (fp2+fm2): the reference's compiled code fuses
+    // the multiply of base (2*f0*(1-ratio)) for d <= 4 and the multiply
+    // ratio*(fp+fm) for d >= 5 (pinned against the reference kernel's output).
     double key = -1.0;
     if (lane < d) {
-      const double base = __dmul_rn(__dmul_rn(S.fv[0], 2.0), __dsub_rn(1.0, rule.ratio));
+      const double f02 = __dmul_rn(S.fv[0], 2.0), omr = __dsub_rn(1.0, rule.ratio);
       const double fp = S.fv[1 + 2 * lane], fm = S.fv[2 + 2 * lane];
       const double fp2 = S.fv[1 + 2 * lane + 2 * d], fm2 = S.fv[2 + 2 * lane + 2 * d];
-      const double fd = fabs(__dsub_rn(__fma_rn(rule.ratio, __dadd_rn(fp, fm), base), __dadd_rn(fp2, fm2)));
+      const double X = __dadd_rn(fp, fm);
+      const double s = (d <= 4) ? __fma_rn(f02, omr, __dmul_rn(rule.ratio, X))
+                                : __fma_rn(rule.ratio, X, __dmul_rn(f02, omr));
+      const double fd = fabs(__dsub_rn(s, __dadd_rn(fp2, fm2)));
       if (fd > 0.0) key = fd;
     }
     double kmax = key;

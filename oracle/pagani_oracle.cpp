@@ -449,14 +449,19 @@ static EvalOut eval_region(const Rule& R, const Prepared& P, const double* lows,
   // Fourth differences and split axis (Sample.cuh:194-218).
   int bisect = maxDim;
   {
+    // base + ratio*(fp+fm) - (fp2+fm2), with the multiply that the
+    // reference's compiled code fuses: base's for d <= 4, ratio's for d >= 5.
     const double q = R.G[1] / R.G[0];
     const double ratio = q * q;
-    const double base = (f64[0] * 2) * (1 - ratio);
+    const double f02 = f64[0] * 2, omr = 1 - ratio;
+    const double base = f02 * omr;
     double maxdiff = 0;
     for (int k = 0; k < d; ++k) {
       const double fp = f64[1 + 2 * k], fm = f64[2 + 2 * k];
       const double fp2 = f64[1 + 2 * k + 2 * d], fm2 = f64[2 + 2 * k + 2 * d];
-      const double fd = std::fabs(std::fma(ratio, fp + fm, base) - (fp2 + fm2));
+      const double X = fp + fm;
+      const double s = (d <= 4) ? std::fma(f02, omr, ratio * X) : std::fma(ratio, X, base);
+      const double fd = std::fabs(s - (fp2 + fm2));
       if (fd > maxdiff) {
         maxdiff = fd;
         bisect = k;
