@@ -40,7 +40,7 @@ WORKLOAD = "batched PAGANI: 4096 pre-screened mixed Genz integrals, dim 2..8, 6 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--steps", type=int, default=1)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--count", type=int, default=4096)

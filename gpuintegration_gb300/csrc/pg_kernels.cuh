@@ -106,7 +106,7 @@ template <int MAXD>
 struct EvalWarpSmem {
   EvalTrieSmem<MAXD> trie;
   IntegralDesc desc;
-  double tab[MAXD * kCodesPerDim];
+  double tab[MAXD * kCodesPerDim];  // (tab and fac double as the reduction area of the d > 8 kernel)
   double fac[MAXD * kCodesPerDim];  // per-axis factors of separable integrands
   double fv[64];
   double lo[MAXD];
@@ -237,30 +237,41 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
         }
       }
     }
-    // Shuffle-down trees (Sample.cuh:49-59), both halves.
+    // The reference's block sum (Sample.cuh:49-83) per rule: a shuffle-down
+    // tree over each 32-lane half (offsets 16, 8, 4, 2, 1), then
+    // (half0 + 0) + half1.  The same additions in the same pairs are done here
+    // level by level on shared memory, packing the 10 trees' additions of a
+    // level into as few warp instructions as possible.
+    double* red;  // free by now: the trie buffer (d <= 8 kernel) or tab + fac (352 doubles)
+    if constexpr (MAXD <= kTrieMaxDim)
+      red = S.trie.a;
+    else
+      red = S.tab;
+    __syncwarp();
+    red[0 * 32 + lane] = sa0;
+    red[1 * 32 + lane] = sa1;
+    red[2 * 32 + lane] = sa2;
+    red[3 * 32 + lane] = sa3;
+    red[4 * 32 + lane] = sa4;
+    red[5 * 32 + lane] = sb0;
+    red[6 * 32 + lane] = sb1;
+    red[7 * 32 + lane] = sb2;
+    red[8 * 32 + lane] = sb3;
+    red[9 * 32 + lane] = sb4;
+    __syncwarp();
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
-      sa0 = __dadd_rn(sa0, __shfl_down_sync(full, sa0, off));
-      sa1 = __dadd_rn(sa1, __shfl_down_sync(full, sa1, off));
-      sa2 = __dadd_rn(sa2, __shfl_down_sync(full, sa2, off));
-      sa3 = __dadd_rn(sa3, __shfl_down_sync(full, sa3, off));
-      sa4 = __dadd_rn(sa4, __shfl_down_sync(full, sa4, off));
-      sb0 = __dadd_rn(sb0, __shfl_down_sync(full, sb0, off));
-      sb1 = __dadd_rn(sb1, __shfl_down_sync(full, sb1, off));
-      sb2 = __dadd_rn(sb2, __shfl_down_sync(full, sb2, off));
-      sb3 = __dadd_rn(sb3, __shfl_down_sync(full, sb3, off));
-      sb4 = __dadd_rn(sb4, __shfl_down_sync(full, sb4, off));
+      for (int t = lane; t < 10 * off; t += 32) {
+        const int q = t / off, i = t - q * off;
+        red[q * 32 + i] = __dadd_rn(red[q * 32 + i], red[q * 32 + i + off]);
+      }
+      __syncwarp();
     }
-    // Block sum: (warp0 + 0) + warp1, broadcast from lane 0.
-    const double s0 = __shfl_sync(full, __dadd_rn(__dadd_rn(sa0, 0.0), sb0), 0);
-    const double s1 = __shfl_sync(full, __dadd_rn(__dadd_rn(sa1, 0.0), sb1), 0);
-    const double s2 = __shfl_sync(full, __dadd_rn(__dadd_rn(sa2, 0.0), sb2), 0);
-    const double s3 = __shfl_sync(full, __dadd_rn(__dadd_rn(sa3, 0.0), sb3), 0);
-    const double s4 = __shfl_sync(full, __dadd_rn(__dadd_rn(sa4, 0.0), sb4), 0);
+    if (lane < 5) red[320 + lane] = __dadd_rn(__dadd_rn(red[lane * 32], 0.0), red[(5 + lane) * 32]);
+    __syncwarp();
+    const double s0 = red[320], s1 = red[321], s2 = red[322], s3 = red[323], s4 = red[324];
     __syncwarp();
 
-    // Split axis from the fourth differences (Sample.cuh:194-218): the first
-    // axis whose difference is the largest, if positive; else the widest axis.
     // base + ratio*(fp+fm) - (fp2+fm2): the reference's compiled code fuses
     // the multiply of base (2*f0*(1-ratio)) for d <= 4 and the multiply
     // ratio*(fp+fm) for d >= 5 (pinned against the reference kernel's output).
@@ -298,15 +309,22 @@ static __global__ void __launch_bounds__(kEvalWarps * 32)
       m = fmax(m, o);
     }
     const double e1 = __shfl_sync(full, m, 0), e2 = __shfl_sync(full, m, 1), e3 = __shfl_sync(full, m, 2);
+    // Region volume and widest axis (Phases.cuh:329-348): the side lengths in
+    // parallel, the product in axis order (1.0 * r0 = r0), and the widest-axis
+    // comparison on the bit patterns (side lengths are non-negative).
+    if (lane < d) S.up[lane] = __dsub_rn(S.up[lane], S.lo[lane]);
+    __syncwarp();
     if (lane == 0) {
-      double vol = 1.0, maxr = 0.0;
+      double vol = S.up[0];
+      long long maxbits = __double_as_longlong(vol);
       int maxdim = 0;
-      for (int k = 0; k < d; ++k) {
-        const double rk = __dsub_rn(S.up[k], S.lo[k]);
+      for (int k = 1; k < d; ++k) {
+        const double rk = S.up[k];
         vol = __dmul_rn(vol, rk);
-        if (rk > maxr) {
+        const long long b = __double_as_longlong(rk);
+        if (b > maxbits) {
           maxdim = k;
-          maxr = rk;
+          maxbits = b;
         }
       }
       est[r] = __dmul_rn(vol, s0);
