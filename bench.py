@@ -34,6 +34,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "integrals/s at rel err <=1e-6, batched vs plain PAGANI on 1 GB300; p50/p99 latency"
+# DRAM traffic of an evaluation launch over its algorithmic bytes, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a batched launch.
+DRAM_OVER_ALGORITHMIC = 1828488704 / 1800148656
 WORKLOAD = "batched PAGANI: 4096 pre-screened mixed Genz integrals, dim 2..8, 6 families, epsrel log-U[1e-7,1e-4]"
 
 
@@ -44,7 +47,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--count", type=int, default=4096)
-    p.add_argument("--plain-sample", type=int, default=512)
+    p.add_argument("--plain-sample", type=int, default=256)
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--max-regions", type=int, default=1 << 26)
     p.add_argument("--config", type=int, default=4, choices=[3, 4, 5],
@@ -114,41 +117,43 @@ def run_mcubes(args):
 
 
 # ---------------------------------------------------------------------------
-def flops_per_point(family, d):
+def _feval(d):
+    return 1 + 8 * d + 2 * d * (d - 1) + 4 * d * (d - 1) + 4 * d * (d - 1) * (d - 2) // 3 + (1 << d)
+
+
+def ops_per_point(family, d):
+    """Algorithmic FP64 operations (add, mul, FMA, compare, one per libm call)
+    per evaluation point of the library's algorithm."""
     import gpuintegration_gb300 as pg
     if family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT):
-        f = d - 1  # product of the per-axis factors
+        f = 1 if d <= 8 else d - 1  # last product of the prefix trie (d <= 8) or the pointwise product
     elif family == pg.OSCILLATORY:
-        f = 2 * d + 1
+        f = d + 1
     elif family == pg.CORNER_PEAK:
-        e, muls, sq = d + 1, 0, 0
+        e, muls = d + 1, 0
         while e:
-            if e & 1:
-                muls += 1
+            muls += (e & 1) + (1 if e > 1 else 0)
             e >>= 1
-            if e:
-                sq += 1
-        f = 2 * d + muls + sq + 1
+        f = d + muls + 1
     else:
-        f = 2 * d + 1
-    return f + 10  # five rule sums (FMA = 2 flops)
+        f = d + 1
+    return f + 5  # five rule sums, one FMA each
 
 
-def flops_per_region(family, d):
+def ops_per_region(family, d):
     import gpuintegration_gb300 as pg
-    factor = {pg.PRODUCT_PEAK: 4, pg.GAUSSIAN: 4, pg.C0: 3, pg.DISCONTINUOUS: 2, pg.PRODUCT: 0}.get(family, 0)
-    return 11 * d * (3 + factor) + 60 + (6 * d + 3) + 114 + 2 * d
+    sep = family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT)
+    factor = {pg.PRODUCT_PEAK: 3, pg.GAUSSIAN: 4, pg.C0: 3, pg.DISCONTINUOUS: 2, pg.PRODUCT: 0}.get(family, 0)
+    trie = sum(_feval(k) for k in range(2, d)) if (sep and d <= 8) else 0
+    return 11 * d * (2 + factor) + trie + 320 + (5 * d + 2) + 113 + d
 
 
-def algorithmic_flops(cases, results):
-    import gpuintegration_gb300 as pg
-    lib = pg.load_library()
+def algorithmic_ops(cases, results):
     tot = 0.0
     for c, r in zip(cases, results):
         f = c.integrand
-        fe = lib.pg_feval(f.ndim)
-        regions = r.neval // fe
-        tot += r.neval * flops_per_point(f.family, f.ndim) + regions * flops_per_region(f.family, f.ndim)
+        regions = r.neval // _feval(f.ndim)
+        tot += r.neval * ops_per_point(f.family, f.ndim) + regions * ops_per_region(f.family, f.ndim)
     return tot
 
 
@@ -338,23 +343,27 @@ def main():
     value = world * converged / dev_s
     e2e = world * converged / wall_s
     lat_all = np.concatenate(lat)
-    # Roofline of the dominant kernel (region evaluation, FP64 pipe).
-    alg = algorithmic_flops(cases, results) * args.steps
+    # Roofline of the dominant kernel (region evaluation, FP64 pipe), in FP64
+    # operations per second against the measured FP64 FMA instruction rate.
+    alg = algorithmic_ops(cases, results) * args.steps
     achieved = alg / (st.eval_ms / 1000.0) / 1e12
-    peak = ctx.probe_fp64_peak()
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "eval_kernel_dram.txt")
-    if os.path.exists(prof):
-        for line in open(prof):
-            if line.startswith("dram_bytes_per_eval_point:"):
-                per_pt = float(line.split(":")[1])
-                traffic = per_pt * (st.points_evaluated / max(st.eval_launches, 1))
-    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+    peak = ctx.probe_fp64_peak() / 2.0
+    # DRAM bytes per evaluation launch: the launch's algorithmic bytes (region
+    # bounds in, estimate/error/split axis out, owner index) times the ratio
+    # ncu measured on one batched evaluation launch of this workload (14.27M
+    # regions of the first 4096 integrals, iteration 8: 1.830 GB read+written
+    # against 1.800 GB algorithmic).
+    alg_bytes_per_launch = st.eval_bytes / max(st.eval_launches, 1)
+    traffic = alg_bytes_per_launch * DRAM_OVER_ALGORITHMIC
+    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "FP64 Top/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "eval_kernel",
-            "peak_source": "measured FP64 FMA rate of this GPU (pg_probe_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
-            "algorithmic_flops_per_step": alg / args.steps,
+            "peak_source": "measured FP64 FMA instruction rate of this GPU (pg_probe_fp64_peak, TFLOP/s / 2); "
+                           "MEASURED_PEAKS.json has no FP64 figure",
+            "algorithmic_ops_per_step": alg / args.steps,
+            "algorithmic_bytes_per_launch": alg_bytes_per_launch,
             "eval_ms_per_step": st.eval_ms / args.steps, "stage_ms_per_step": st.stage_ms / args.steps,
-            "stage_gbs": (st.stage_bytes / max(st.stage_ms, 1e-9)) / 1e6}
+            "stage_gbs": (st.stage_bytes / max(st.stage_ms, 1e-9)) / 1e6,
+            "autotuned_launch": {"warps_per_block": list(st.tune_warps), "ctas_per_sm": list(st.tune_ctas_per_sm)}}
     line = {"metric": METRIC, "value": value, "unit": "integrals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -378,8 +387,23 @@ def main():
         t0 = time.perf_counter()
         ctx.batch_integrate([c.integrand for c in sub], [c.epsrel for c in sub], 0.0, options=opt)
         batch_s = time.perf_counter() - t0
-        line["plain"] = {"sample": ns, "plain_integrals_per_s": ns / plain_s, "batched_integrals_per_s": ns / batch_s,
+        line["plain"] = {"sample": f"first {ns} integrals of the workload",
+                         "plain_integrals_per_s": ns / plain_s, "batched_integrals_per_s": ns / batch_s,
                          "batched_over_plain": plain_s / batch_s}
+        # Where batching pays: the light integrals (<= 20000 regions when screened), whose plain
+        # runs are bound by per-iteration launches and synchronisation rather than by FP64 work.
+        screen = json.load(open(os.path.join(ROOT, "tests", "golden", "config4_screen.json")))
+        light = [c for c, nr in zip(cases, screen["nregions"]) if nr <= 20000][:1024]
+        t0 = time.perf_counter()
+        for c in light:
+            ctx.integrate(c.integrand, c.epsrel, 0.0)
+        pl = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctx.batch_integrate([c.integrand for c in light], [c.epsrel for c in light], 0.0, options=opt)
+        bl = time.perf_counter() - t0
+        line["plain_light"] = {"sample": f"first {len(light)} integrals with <= 20000 screened regions",
+                               "plain_integrals_per_s": len(light) / pl, "batched_integrals_per_s": len(light) / bl,
+                               "batched_over_plain": pl / bl}
         # CPU baseline: the oracle on all host cores, bounded sample, extrapolated by evaluation count.
         cpu = cpu_leg(cases, args.cpu_seconds)
         total_pts = sum(r.neval for r in results)

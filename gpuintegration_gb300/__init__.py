@@ -68,7 +68,9 @@ class PgStats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_uint64), ("eval_launches", ctypes.c_uint64),
                 ("regions_evaluated", ctypes.c_uint64), ("points_evaluated", ctypes.c_uint64),
                 ("eval_ms", ctypes.c_double), ("stage_ms", ctypes.c_double), ("stage_bytes", ctypes.c_uint64),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("tune_warps", ctypes.c_int32 * 2), ("tune_ctas_per_sm", ctypes.c_int32 * 2),
+                ("eval_bytes", ctypes.c_uint64)]
 
 
 class PgMcubesOptions(ctypes.Structure):

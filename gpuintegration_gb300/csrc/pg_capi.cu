@@ -125,7 +125,7 @@ void pg_options_default(pg_options* opt) {
   opt->max_iters = 700;
   opt->device_mem_model = 16e9;
   opt->max_regions = 0;
-  opt->eval_mode = PG_EVAL_REFERENCE_ORDER;
+  opt->eval_mode = 0;
 }
 
 int pg_feval(int ndim) {
@@ -184,6 +184,10 @@ int pg_context_set_profiling(pg_context* ctx, int on) {
 int pg_context_stats(const pg_context* ctx, pg_stats* out) {
   if (!ctx || !out) return PG_BAD_ARG;
   *out = ctx->eng->stats;
+  for (int c = 0; c < 2; ++c) {
+    out->tune_warps[c] = ctx->eng->tune[c].warps;
+    out->tune_ctas_per_sm[c] = ctx->eng->tune[c].ctas_per_sm;
+  }
   return PG_OK;
 }
 
@@ -221,6 +225,7 @@ int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double e
   jobs[0].epsrel = epsrel;
   jobs[0].epsabs = epsabs;
   if (opt) jobs[0].opt = *opt; else pg_options_default(&jobs[0].opt);
+  if (jobs[0].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
   if (jobs[0].opt.max_iters <= 0) jobs[0].opt.max_iters = 700;
   rc = ctx->eng->run(jobs, pg::launch_family_eval);
   if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
@@ -248,6 +253,7 @@ int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand
     jobs[i].epsrel = epsrel[i];
     jobs[i].epsabs = epsabs[i];
     if (opt) jobs[i].opt = *opt; else pg_options_default(&jobs[i].opt);
+    if (jobs[i].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
     if (jobs[i].opt.max_iters <= 0) jobs[i].opt.max_iters = 700;
   }
   pg::RunPolicy pol;
@@ -280,6 +286,7 @@ int pg_serve(pg_context* ctx, uint64_t count, const pg_integrand* fs, const doub
     jobs[i].epsrel = epsrel[i];
     jobs[i].epsabs = epsabs[i];
     if (opt) jobs[i].opt = *opt; else pg_options_default(&jobs[i].opt);
+    if (jobs[i].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
     if (jobs[i].opt.max_iters <= 0) jobs[i].opt.max_iters = 700;
   }
   pg::RunPolicy pol;
@@ -300,7 +307,7 @@ int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const dou
                                uint64_t n, const double* d_left, const double* d_length, double* d_est, double* d_err,
                                int32_t* d_bisect, int32_t eval_mode) {
   if (!ctx || !f) return set_err(ctx, PG_BAD_ARG, "null argument");
-  (void)eval_mode;
+  if (eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
   Guard g(ctx);
   pg::IntegralDesc D;
   std::string why;
@@ -311,17 +318,11 @@ int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const dou
   return PG_OK;
 }
 
-int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs, uint64_t n,
-                        const double* left, const double* length, double* est, double* err, int32_t* bisect,
-                        int32_t eval_mode) {
-  if (!ctx || !f || (n && (!left || !length || !est || !err || !bisect)))
-    return set_err(ctx, PG_BAD_ARG, "null argument");
-  (void)eval_mode;
-  Guard g(ctx);
-  pg::IntegralDesc D;
-  std::string why;
-  int rc = pg::prepare_desc(*f, lows, highs, &D, &why);
-  if (rc != PG_OK) return set_err(ctx, rc, why);
+// Host-buffer region evaluation shared by the family and user-integrand entry points.
+static int evaluate_host(pg_context* ctx, const pg::IntegralDesc& D, uint64_t n, const double* left,
+                         const double* length, double* est, double* err, int32_t* bisect,
+                         const pg::EvalLauncher& launch) {
+  int rc;
   if (n == 0) return PG_OK;
   const size_t nd = n * (size_t)D.d;
   CAPI_ENSURE(ctx, ctx->s_left, nd * 8);
@@ -333,7 +334,7 @@ int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lo
   CAPI_TRY(ctx, cudaMemcpyAsync(ctx->s_left.p, left, nd * 8, cudaMemcpyHostToDevice, s), "upload");
   CAPI_TRY(ctx, cudaMemcpyAsync(ctx->s_len.p, length, nd * 8, cudaMemcpyHostToDevice, s), "upload");
   rc = ctx->eng->evaluate(D, n, (const double*)ctx->s_left.p, (const double*)ctx->s_len.p, n, (double*)ctx->s_est.p,
-                          (double*)ctx->s_err.p, (int32_t*)ctx->s_bis.p, pg::launch_family_eval);
+                          (double*)ctx->s_err.p, (int32_t*)ctx->s_bis.p, launch);
   if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
   CAPI_TRY(ctx, cudaMemcpyAsync(est, ctx->s_est.p, n * 8, cudaMemcpyDeviceToHost, s), "download");
   CAPI_TRY(ctx, cudaMemcpyAsync(err, ctx->s_err.p, n * 8, cudaMemcpyDeviceToHost, s), "download");
@@ -342,6 +343,66 @@ int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lo
   ctx->eng->stats.h2d_bytes += 2 * nd * 8;
   ctx->eng->stats.d2h_bytes += n * 20;
   return PG_OK;
+}
+
+int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs, uint64_t n,
+                        const double* left, const double* length, double* est, double* err, int32_t* bisect,
+                        int32_t eval_mode) {
+  if (!ctx || !f || (n && (!left || !length || !est || !err || !bisect)))
+    return set_err(ctx, PG_BAD_ARG, "null argument");
+  if (eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+  Guard g(ctx);
+  pg::IntegralDesc D;
+  std::string why;
+  int rc = pg::prepare_desc(*f, lows, highs, &D, &why);
+  if (rc != PG_OK) return set_err(ctx, rc, why);
+  return evaluate_host(ctx, D, n, left, length, est, err, bisect, pg::launch_family_eval);
+}
+
+// ---------------------------------------------------------------------------
+// User integrands: the caller's launcher instantiates the evaluation kernel
+// for its functor; everything else is the library's iteration.
+// ---------------------------------------------------------------------------
+static pg::EvalLauncher user_launcher(pg_eval_launcher fn, void* user) {
+  return [fn, user](const pg::EvalLaunch& L) -> cudaError_t {
+    const pg_eval_args a = pg::eval_args_of(L);
+    return (cudaError_t)fn(&a, user);
+  };
+}
+
+int pg_integrate_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user, double epsrel,
+                          double epsabs, const double* lows, const double* highs, const pg_options* opt,
+                          pg_result* out) {
+  if (!ctx || !launch || !out) return set_err(ctx, PG_BAD_ARG, "null argument");
+  int rc = validate_eps(ctx, epsrel, epsabs);
+  if (rc != PG_OK) return rc;
+  Guard g(ctx);
+  std::vector<pg::Job> jobs(1);
+  std::string why;
+  rc = pg::prepare_user_desc(ndim, lows, highs, &jobs[0].desc, &why);
+  if (rc != PG_OK) return set_err(ctx, rc, why);
+  jobs[0].epsrel = epsrel;
+  jobs[0].epsabs = epsabs;
+  if (opt) jobs[0].opt = *opt; else pg_options_default(&jobs[0].opt);
+  if (jobs[0].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+  if (jobs[0].opt.max_iters <= 0) jobs[0].opt.max_iters = 700;
+  rc = ctx->eng->run(jobs, user_launcher(launch, user));
+  if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
+  *out = jobs[0].res;
+  return out->status == 0 ? PG_OK : PG_NOT_CONVERGED;
+}
+
+int pg_evaluate_regions_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user,
+                                 const double* lows, const double* highs, uint64_t n, const double* left,
+                                 const double* length, double* est, double* err, int32_t* bisect) {
+  if (!ctx || !launch || (n && (!left || !length || !est || !err || !bisect)))
+    return set_err(ctx, PG_BAD_ARG, "null argument");
+  Guard g(ctx);
+  pg::IntegralDesc D;
+  std::string why;
+  int rc = pg::prepare_user_desc(ndim, lows, highs, &D, &why);
+  if (rc != PG_OK) return set_err(ctx, rc, why);
+  return evaluate_host(ctx, D, n, left, length, est, err, bisect, user_launcher(launch, user));
 }
 
 int pg_two_level(pg_context* ctx, uint64_t n, const double* est, const double* err, const double* parent_est,
@@ -615,6 +676,31 @@ int pg_mcubes_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, d
     if (!ctx->mc) return set_err(ctx, PG_OOM, "m-Cubes state");
   }
   rc = pg::mcubes_run(ctx->mc, D, epsrel, epsabs, o, out, &why);
+  if (rc < 0) return set_err(ctx, rc, why);
+  return out->status == 0 ? PG_OK : PG_NOT_CONVERGED;
+}
+
+int pg_mcubes_integrate_launcher(pg_context* ctx, int32_t ndim, pg_mcubes_launcher launch, void* user,
+                                 double epsrel, double epsabs, const double* lows, const double* highs,
+                                 const pg_mcubes_options* opt, pg_result* out) {
+  if (!ctx || !launch || !out) return set_err(ctx, PG_BAD_ARG, "null argument");
+  int rc = validate_eps(ctx, epsrel, epsabs);
+  if (rc != PG_OK) return rc;
+  Guard g(ctx);
+  pg_mcubes_options o;
+  if (opt) o = *opt; else pg_mcubes_options_default(&o);
+  pg::IntegralDesc D;
+  std::string why;
+  rc = pg::prepare_user_desc(ndim, lows, highs, &D, &why);
+  if (rc != PG_OK) return set_err(ctx, rc, why);
+  if (!ctx->mc) {
+    ctx->mc = pg::mcubes_create(ctx->eng);
+    if (!ctx->mc) return set_err(ctx, PG_OOM, "m-Cubes state");
+  }
+  const pg::McubesLauncher L = [launch, user](const pg_mcubes_args& a) -> cudaError_t {
+    return (cudaError_t)launch(&a, user);
+  };
+  rc = pg::mcubes_run(ctx->mc, D, epsrel, epsabs, o, out, &why, L);
   if (rc < 0) return set_err(ctx, rc, why);
   return out->status == 0 ? PG_OK : PG_NOT_CONVERGED;
 }

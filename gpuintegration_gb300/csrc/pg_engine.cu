@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <thread>
 #include <cstdio>
@@ -127,6 +128,16 @@ int prepare_desc(const pg_integrand& f, const double* lows, const double* highs,
   D.unit = unit;
   *out = D;
   return PG_OK;
+}
+
+int prepare_user_desc(int ndim, const double* lows, const double* highs, IntegralDesc* out, std::string* why) {
+  pg_integrand f;
+  std::memset(&f, 0, sizeof f);
+  f.family = FAM_CONSTANT;
+  f.ndim = ndim;
+  const int rc = prepare_desc(f, lows, highs, out, why);
+  if (rc == PG_OK) out->family = FAM_USER;
+  return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -269,17 +280,20 @@ void Engine::record(cudaEvent_t a, cudaEvent_t b, double* acc) {
 int Engine::evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length,
                      uint64_t stride, double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch) {
   int rc;
+  if ((rc = autotune()) != PG_OK) return rc;
   if ((rc = ensure(descs_, sizeof(IntegralDesc))) != PG_OK) return rc;
   PG_TRY(cudaMemcpyAsync(descs_.p, &desc, sizeof desc, cudaMemcpyHostToDevice, stream_), "desc upload");
   if (n == 0) return PG_OK;
+  const EvalTune& tn = tune[desc.d <= 8 ? 0 : 1];
   EvalLaunch L{d_left, d_length, n, stride, nullptr, (const IntegralDesc*)descs_.p, &rule_, d_est, d_err, d_bisect,
-               desc.d, num_sms, stream_};
+               desc.d, num_sms, stream_, tn.warps, tn.ctas_per_sm};
   if (profiling) cudaEventRecord(ev_[0], stream_);
   PG_TRY(launch(L), "evaluation launch");
   stats.launches++;
   stats.eval_launches++;
   stats.regions_evaluated += n;
   stats.points_evaluated += n * (uint64_t)rule_.feval[desc.d];
+  stats.eval_bytes += n * (16ull * desc.d + 20ull);  // bounds in; estimate, error, split axis out
   if (profiling) {
     cudaEventRecord(ev_[1], stream_);
     PG_TRY(cudaEventSynchronize(ev_[1]), "evaluation");
@@ -473,6 +487,7 @@ int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int max
 int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPolicy& policy) {
   int rc;
   PG_TRY(cudaSetDevice(device), "cudaSetDevice");
+  if ((rc = autotune()) != PG_OK) return rc;
   const uint32_t njobs = (uint32_t)jobs.size();
   if (njobs == 0) return PG_OK;
   int maxd = 2;
@@ -676,15 +691,19 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     PG_TRY(cudaMemcpyAsync(live_.p, hl, live.size() * 4, cudaMemcpyHostToDevice, stream_), "live upload");
     stats.h2d_bytes += njobs * sizeof(SegDesc) + nchunks * sizeof(ChunkRef) + live.size() * 4;
     // 1. evaluation
+    const EvalTune& tn = tune[maxd <= 8 ? 0 : 1];
     EvalLaunch L{(const double*)left_[cur].p, (const double*)len_[cur].p, N, reg_cap_[cur],
                  (const uint32_t*)owner_[cur].p, (const IntegralDesc*)descs_.p, &rule_, (double*)est_.p,
-                 (double*)err_a_.p, (int32_t*)bisect_.p, maxd, num_sms, stream_};
+                 (double*)err_a_.p, (int32_t*)bisect_.p, maxd, num_sms, stream_, tn.warps, tn.ctas_per_sm};
     if (profiling) cudaEventRecord(ev_[0], stream_);
     PG_TRY(launch(L), "evaluation launch");
     stats.launches++;
     stats.eval_launches++;
     stats.regions_evaluated += N;
-    for (uint32_t j : live) stats.points_evaluated += jobs[j].n * (uint64_t)rule_.feval[jobs[j].desc.d];
+    for (uint32_t j : live) {
+      stats.points_evaluated += jobs[j].n * (uint64_t)rule_.feval[jobs[j].desc.d];
+      stats.eval_bytes += jobs[j].n * (16ull * jobs[j].desc.d + 24ull);  // + the 4-byte owner of a shared list
+    }
     if (profiling) cudaEventRecord(ev_[1], stream_);
     // 2. two-level error + classification + partial sums; 3. per-integral totals
     two_level_kernel<<<(unsigned)nchunks, kRedThreads, 0, stream_>>>(
@@ -886,30 +905,83 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   return PG_OK;
 }
 
+int Engine::autotune() {
+  const EvalLauncher launch = launch_family_eval;
+  if (tuned) return PG_OK;
+  const char* env = std::getenv("PG_AUTOTUNE");
+  tuned = true;
+  if (env && env[0] == '0') return PG_OK;
+  // One synthetic list per kernel class: 8-D and 10-D Gaussians on 24576
+  // regions of mixed sizes (the work of one region does not depend on its
+  // size, so the list only has to fill the GPU several times over).
+  const int dims[2] = {8, 10};
+  const int warps_c[2] = {4, 8};
+  const int ctas_c[3] = {8, 16, 32};
+  const uint64_t n = 24576;
+  int rc;
+  for (int cls = 0; cls < 2; ++cls) {
+    const int d = dims[cls];
+    std::vector<double> left((size_t)d * n), len((size_t)d * n);
+    uint64_t state = 0x9E3779B97F4A7C15ull * (cls + 1);
+    for (size_t i = 0; i < left.size(); ++i) {
+      state = state * 6364136223846793005ull + 1442695040888963407ull;
+      const int depth = (int)((state >> 33) % 6);
+      const double h = std::ldexp(1.0, -depth);
+      const uint64_t cells = 1ull << depth;
+      len[i] = h;
+      left[i] = (double)((state >> 20) % cells) * h;
+    }
+    DevBuf dl, dn, de, dr, db;
+    if ((rc = ensure(dl, left.size() * 8)) != PG_OK || (rc = ensure(dn, len.size() * 8)) != PG_OK ||
+        (rc = ensure(de, n * 8)) != PG_OK || (rc = ensure(dr, n * 8)) != PG_OK || (rc = ensure(db, n * 4)) != PG_OK)
+      return rc;
+    pg_integrand f;
+    std::memset(&f, 0, sizeof f);
+    f.family = FAM_GAUSSIAN;
+    f.ndim = d;
+    for (int k = 0; k < d; ++k) {
+      f.a[k] = 3.0 + 0.25 * k;
+      f.u[k] = 0.5;
+    }
+    IntegralDesc D;
+    prepare_desc(f, nullptr, nullptr, &D, nullptr);
+    PG_TRY(cudaMemcpyAsync(dl.p, left.data(), left.size() * 8, cudaMemcpyHostToDevice, stream_), "tune upload");
+    PG_TRY(cudaMemcpyAsync(dn.p, len.data(), len.size() * 8, cudaMemcpyHostToDevice, stream_), "tune upload");
+    if ((rc = ensure(descs_, sizeof(IntegralDesc))) != PG_OK) return rc;
+    PG_TRY(cudaMemcpyAsync(descs_.p, &D, sizeof D, cudaMemcpyHostToDevice, stream_), "tune upload");
+    EvalTune best;
+    best.ms = 1e30;
+    for (int w : warps_c)
+      for (int c : ctas_c) {
+        EvalLaunch L{(const double*)dl.p, (const double*)dn.p, n, n, nullptr, (const IntegralDesc*)descs_.p, &rule_,
+                     (double*)de.p, (double*)dr.p, (int32_t*)db.p, d, num_sms, stream_, w, c};
+        PG_TRY(launch(L), "tune launch");  // warm-up
+        PG_TRY(cudaEventRecord(ev_[0], stream_), "tune event");
+        for (int rep = 0; rep < 2; ++rep) PG_TRY(launch(L), "tune launch");
+        PG_TRY(cudaEventRecord(ev_[1], stream_), "tune event");
+        PG_TRY(cudaEventSynchronize(ev_[1]), "tune");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+        stats.launches += 3;
+        if (ms < best.ms) {
+          best.ms = ms;
+          best.warps = w;
+          best.ctas_per_sm = c;
+        }
+      }
+    tune[cls] = best;
+    DevBuf* bufs[] = {&dl, &dn, &de, &dr, &db};
+    for (DevBuf* b : bufs) cudaFree(b->p);
+  }
+  return PG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Evaluation launcher for the C ABI families.
 // ---------------------------------------------------------------------------
-template <int MAXD>
-static cudaError_t launch_family_eval_t(const EvalLaunch& L) {
-  const size_t smem = sizeof(EvalWarpSmem<MAXD>) * kEvalWarps;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(eval_kernel<MAXD, FamilyFn>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
-  const uint64_t want = div_up(L.n, kEvalWarps);
-  const uint64_t cap = (uint64_t)L.num_sms * 32;
-  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(want, cap));
-  eval_kernel<MAXD, FamilyFn><<<grid, kEvalWarps * 32, smem, L.stream>>>(
-      L.left, L.length, L.n, L.stride, L.owner, L.descs, *L.rule, FamilyFn{}, L.est, L.err, L.bisect);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_family_eval(const EvalLaunch& L) {
-  if (L.maxd <= 8) return launch_family_eval_t<8>(L);
-  return launch_family_eval_t<16>(L);
+  const pg_eval_args a = eval_args_of(L);
+  return L.maxd <= 8 ? launch_eval<8>(a, FamilyFn{}) : launch_eval<16>(a, FamilyFn{});
 }
 
 }  // namespace pg

@@ -35,10 +35,41 @@ struct EvalLaunch {
   int maxd;
   int num_sms;
   cudaStream_t stream;
+  int warps;        // regions per block (warps per CTA)
+  int ctas_per_sm;  // grid cap of the grid-stride evaluation loop
+};
+
+// Launch shape of the evaluation kernel for one kernel class (d <= 8, d > 8),
+// chosen by Engine::autotune.
+struct EvalTune {
+  int warps = 8;
+  int ctas_per_sm = 32;
+  double ms = 0;  // time of the tuning launch with this shape
 };
 
 // Launches the evaluation kernel for some integrand functor type.
 using EvalLauncher = std::function<cudaError_t(const EvalLaunch&)>;
+
+// The same launch as the C ABI's plain argument block.
+inline pg_eval_args eval_args_of(const EvalLaunch& L) {
+  pg_eval_args a;
+  a.left = L.left;
+  a.length = L.length;
+  a.n = L.n;
+  a.stride = L.stride;
+  a.owner = L.owner;
+  a.descs = L.descs;
+  a.rule = L.rule;
+  a.est = L.est;
+  a.err = L.err;
+  a.bisect = L.bisect;
+  a.maxd = L.maxd;
+  a.num_sms = L.num_sms;
+  a.stream = (void*)L.stream;
+  a.warps = L.warps;
+  a.ctas_per_sm = L.ctas_per_sm;
+  return a;
+}
 
 // The launcher of the C ABI families.
 cudaError_t launch_family_eval(const EvalLaunch& L);
@@ -101,6 +132,9 @@ struct RunPolicy {
 // Prepares an IntegralDesc from the C ABI description (host, no contraction).
 int prepare_desc(const pg_integrand& f, const double* lows, const double* highs, IntegralDesc* out, std::string* why);
 
+// Descriptor of a caller's functor integrand: the integration box only.
+int prepare_user_desc(int ndim, const double* lows, const double* highs, IntegralDesc* out, std::string* why);
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -118,6 +152,14 @@ class Engine {
   // Evaluates caller-given regions (device pointers, SoA stride n).
   int evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length, uint64_t stride,
                double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch);
+
+  // Times the candidate launch shapes of the evaluation kernel on a synthetic
+  // region list per kernel class and keeps the fastest (once per context).
+  // Always with the library's own families: a caller's functor is never run
+  // outside its integration box.
+  int autotune();
+  EvalTune tune[2];
+  bool tuned = false;
 
   cudaStream_t stream() const { return stream_; }
   const RuleDev& rule() const { return rule_; }

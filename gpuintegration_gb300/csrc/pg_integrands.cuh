@@ -25,7 +25,8 @@ enum Family : int32_t {
   FAM_NAN = 8,
   FAM_BOX = 9,
   FAM_FUN6 = 10,
-  FAM_COUNT = 11
+  FAM_COUNT = 11,
+  FAM_USER = 64  // a caller's functor (C++ layer); never accepted from a pg_integrand
 };
 
 // Everything a kernel needs to know about one integral: its integrand, the

@@ -17,158 +17,14 @@
 //     exponent alpha (1.5 in the reference's GPU code, vegas_utils.cuh:139).
 #include "pg_mcubes.h"
 
+#include "pg_mcubes_kernel.cuh"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 namespace pg {
-
-constexpr int kMcThreads = 256;
-constexpr int kMcBlocks = 1024;
-constexpr double kTiny = 1.0e-30;  // vegas_utils.cuh:141
-
-__host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
-  for (int r = 0; r < 10; ++r) {
-    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
-    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
-    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
-    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
-    c[1] = (uint32_t)p1;
-    c[3] = (uint32_t)p0;
-    c[0] = n0;
-    c[2] = n2;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-}
-
-// Uniform double in (0, 1] from 53 random bits.
-__host__ __device__ inline double philox_unit(uint32_t a, uint32_t b) {
-  const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
-  return (double)(m + 1) * 1.1102230246251565404236316680908203125e-16;  // 2^-53
-}
-
-struct McArgs {
-  IntegralDesc desc;
-  int d, ng, npg, nbins;
-  uint64_t ncubes;
-  double dxg, xnd, xjac;
-  double regn[kMaxDim], dx[kMaxDim];
-  uint32_t key0, key1, iter;
-  int adapt;
-  const double* xi;   // [d][nbins + 1], xi[j][0] = 0
-  double* bins;       // [d][nbins + 1] sums of f^2 per bin (adapt)
-  double* partial;    // [kMcBlocks][2]
-};
-
-template <int MAXD>
-__global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A) {
-  extern __shared__ __align__(16) double mc_smem[];
-  const int nb1 = A.nbins + 1;
-  double* sxi = mc_smem;                 // d * nb1
-  double* hist = mc_smem + A.d * nb1;    // d * nb1 (adapt)
-  for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) {
-    sxi[i] = A.xi[i];
-    if (A.adapt) hist[i] = 0.0;
-  }
-  __syncthreads();
-  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t nthreads = (uint64_t)kMcBlocks * kMcThreads;
-  const uint64_t per = (A.ncubes + nthreads - 1) / nthreads;
-  const uint64_t c0 = tid * per, c1 = min(A.ncubes, c0 + per);
-  double fbg = 0.0, f2bg = 0.0;
-  for (uint64_t cube = c0; cube < c1; ++cube) {
-    // kg: 1-based interval index per axis, axis 0 most significant (get_indx, vegasT.cuh:136-154)
-    int kg[MAXD];
-    uint64_t q = cube;
-#pragma unroll
-    for (int j = MAXD - 1; j >= 0; --j) {
-      if (j < A.d) {
-        kg[j] = 1 + (int)(q % (uint64_t)A.ng);
-        q /= (uint64_t)A.ng;
-      }
-    }
-    double fb = 0.0, f2b = 0.0;
-    for (int k = 1; k <= A.npg; ++k) {
-      double wgt = A.xjac;
-      double x[MAXD];
-      int ia[MAXD];
-      uint32_t rnd[4] = {0, 0, 0, 0};
-#pragma unroll
-      for (int j = 0; j < MAXD; ++j) {
-        if (j < A.d) {
-          if ((j & 1) == 0) {
-            rnd[0] = (uint32_t)cube;
-            rnd[1] = (uint32_t)k | ((uint32_t)(cube >> 32) << 16);
-            rnd[2] = (uint32_t)(j >> 1);
-            rnd[3] = A.iter;
-            philox4x32_10(rnd, A.key0, A.key1);
-          }
-          const double ran = (j & 1) ? philox_unit(rnd[2], rnd[3]) : philox_unit(rnd[0], rnd[1]);
-          // Setup_Integrand_Eval (vegasT.cuh:173-212)
-          const double xn = __fma_rn(__dsub_rn((double)kg[j], ran), A.dxg, 1.0);
-          const int b = max(min((int)xn, A.nbins), 1);
-          const double* xij = sxi + j * nb1;
-          double xo, rc;
-          if (b > 1) {
-            xo = __dsub_rn(xij[b], xij[b - 1]);
-            rc = __fma_rn(__dsub_rn(xn, (double)b), xo, xij[b - 1]);
-          } else {
-            xo = xij[b];
-            rc = __dmul_rn(__dsub_rn(xn, (double)b), xo);
-          }
-          x[j] = __fma_rn(rc, A.dx[j], A.regn[j]);
-          wgt = __dmul_rn(wgt, __dmul_rn(xo, A.xnd));
-          ia[j] = b;
-        }
-      }
-      const double f = __dmul_rn(wgt, family_eval<MAXD>(A.desc, x));
-      const double f2 = __dmul_rn(f, f);
-      fb = __dadd_rn(fb, f);
-      f2b = __dadd_rn(f2b, f2);
-      if (A.adapt) {
-#pragma unroll
-        for (int j = 0; j < MAXD; ++j)
-          if (j < A.d) atomicAdd(&hist[j * nb1 + ia[j]], f2);
-      }
-    }
-    // per-cube variance term (vegasT.cuh:336-343)
-    f2b = sqrt(__dmul_rn(f2b, (double)A.npg));
-    f2b = __dmul_rn(__dsub_rn(f2b, fb), __dadd_rn(f2b, fb));
-    if (f2b <= 0.0) f2b = kTiny;
-    fbg = __dadd_rn(fbg, fb);
-    f2bg = __dadd_rn(f2bg, f2b);
-  }
-  // Block sums: shuffle-down trees, then the 8 warp results in order.
-  __shared__ double red[2][8];
-#pragma unroll
-  for (int off = 16; off >= 1; off >>= 1) {
-    fbg = __dadd_rn(fbg, __shfl_down_sync(0xffffffffu, fbg, off));
-    f2bg = __dadd_rn(f2bg, __shfl_down_sync(0xffffffffu, f2bg, off));
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) {
-    red[0][warp] = fbg;
-    red[1][warp] = f2bg;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s0 = 0.0, s1 = 0.0;
-    for (int w = 0; w < kMcThreads / 32; ++w) {
-      s0 = __dadd_rn(s0, red[0][w]);
-      s1 = __dadd_rn(s1, red[1][w]);
-    }
-    A.partial[2 * blockIdx.x] = s0;
-    A.partial[2 * blockIdx.x + 1] = s1;
-  }
-  if (A.adapt) {
-    for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) {
-      const double v = hist[i];
-      if (v != 0.0) atomicAdd(&A.bins[i], v);
-    }
-  }
-}
 
 struct McubesState {
   Engine* eng = nullptr;
@@ -215,8 +71,12 @@ int status_of(double est, double err, int it, double epsrel, double epsabs) {
 
 }  // namespace
 
+cudaError_t launch_family_mcubes(const pg_mcubes_args& a) {
+  return a.maxd <= 8 ? launch_mcubes<8>(a, FamilyFn{}) : launch_mcubes<16>(a, FamilyFn{});
+}
+
 int mcubes_run(McubesState* st, const IntegralDesc& D, double epsrel, double epsabs, const pg_mcubes_options& opt,
-               pg_result* out, std::string* why) {
+               pg_result* out, std::string* why, const McubesLauncher& launcher) {
   Engine* E = st->eng;
   const int d = D.d;
   const int nd = opt.nbins > 1 ? opt.nbins : 500;
@@ -267,21 +127,7 @@ int mcubes_run(McubesState* st, const IntegralDesc& D, double epsrel, double eps
     if (why) *why = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? PG_OOM : PG_CUDA_ERROR;
   };
-  static bool attr8 = false, attr16 = false;
-  cudaError_t ce;
-  if (d <= 8 && !attr8) {
-    if ((ce = cudaFuncSetAttribute(mcubes_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-        cudaSuccess)
-      return fail(ce, "cudaFuncSetAttribute");
-    attr8 = true;
-  }
-  if (d > 8 && !attr16) {
-    if ((ce = cudaFuncSetAttribute(mcubes_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-        cudaSuccess)
-      return fail(ce, "cudaFuncSetAttribute");
-    attr16 = true;
-  }
-  if (smem > 200 * 1024) {
+  if (smem > kMcMaxSmem) {
     if (why) *why = "too many bins for this dimension";
     return PG_BAD_ARG;
   }
@@ -316,13 +162,16 @@ int mcubes_run(McubesState* st, const IntegralDesc& D, double epsrel, double eps
     if ((e = cudaMemcpyAsync(st->xi.p, xi.data(), xi.size() * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return fail(e, "grid upload");
     if (adapt && (e = cudaMemsetAsync(st->bins.p, 0, xi.size() * 8, s)) != cudaSuccess) return fail(e, "memset");
-    if (d <= 8)
-      mcubes_kernel<8><<<kMcBlocks, kMcThreads, smem, s>>>(A);
-    else
-      mcubes_kernel<16><<<kMcBlocks, kMcThreads, smem, s>>>(A);
+    pg_mcubes_args la;
+    la.args = &A;
+    la.smem = smem;
+    la.stream = (void*)s;
+    la.maxd = d;
+    la.pad = 0;
+    e = launcher(la);
     E->stats.launches++;
     E->stats.points_evaluated += (uint64_t)calls;
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "m-Cubes launch");
+    if (e != cudaSuccess) return fail(e, "m-Cubes launch");
     if ((e = cudaMemcpyAsync(part.data(), st->partial.p, part.size() * 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
       return fail(e, "readback");
     if (adapt &&

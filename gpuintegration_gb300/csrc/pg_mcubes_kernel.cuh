@@ -1,0 +1,189 @@
+// m-Cubes sampling kernel (stratified VEGAS), shared by the library's
+// integrand families and by the C++ layer's user integrands
+// (include/pagani_gb300.cuh), which instantiate it in their own translation
+// unit.  Restates the sampling of cuda_mcubes::vegas_kernel / vegas_kernelF
+// (cuda/mcubes/vegasT.cuh:136-614):
+//   * the same point map, weights and per-cube variance term;
+//   * random numbers from Philox4x32-10 (Salmon et al., SC'11), keyed by the
+//     seed with counter (cube, sample, axis pair, iteration);
+//   * per-bin sums of f^2 in a shared-memory histogram per block, flushed once
+//     per block, instead of one global atomic per sample and axis;
+//   * a fixed grid of 1024 x 256 threads, each taking a contiguous run of
+//     cubes, and block-tree sums, so the estimate does not depend on the SM count.
+// Every floating-point operation is an explicit IEEE intrinsic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pagani_gb300.h"
+#include "pg_common.cuh"
+#include "pg_integrands.cuh"
+
+namespace pg {
+
+constexpr int kMcThreads = 256;
+constexpr int kMcBlocks = 1024;
+constexpr double kTiny = 1.0e-30;  // vegas_utils.cuh:141
+
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[1] = (uint32_t)p1;
+    c[3] = (uint32_t)p0;
+    c[0] = n0;
+    c[2] = n2;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Uniform double in (0, 1] from 53 random bits.
+__host__ __device__ __forceinline__ double philox_unit(uint32_t a, uint32_t b) {
+  const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+  return (double)(m + 1) * 1.1102230246251565404236316680908203125e-16;  // 2^-53
+}
+
+struct McArgs {
+  IntegralDesc desc;
+  int d, ng, npg, nbins;
+  uint64_t ncubes;
+  double dxg, xnd, xjac;
+  double regn[kMaxDim], dx[kMaxDim];
+  uint32_t key0, key1, iter;
+  int adapt;
+  const double* xi;   // [d][nbins + 1], xi[j][0] = 0
+  double* bins;       // [d][nbins + 1] sums of f^2 per bin (adapt)
+  double* partial;    // [kMcBlocks][2]
+};
+
+template <int MAXD, class Fn>
+__global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A, Fn fn) {
+  extern __shared__ __align__(16) double mc_smem[];
+  const int nb1 = A.nbins + 1;
+  double* sxi = mc_smem;                 // d * nb1
+  double* hist = mc_smem + A.d * nb1;    // d * nb1 (adapt)
+  for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) {
+    sxi[i] = A.xi[i];
+    if (A.adapt) hist[i] = 0.0;
+  }
+  __syncthreads();
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t nthreads = (uint64_t)kMcBlocks * kMcThreads;
+  const uint64_t per = (A.ncubes + nthreads - 1) / nthreads;
+  const uint64_t c0 = tid * per, c1 = min(A.ncubes, c0 + per);
+  double fbg = 0.0, f2bg = 0.0;
+  for (uint64_t cube = c0; cube < c1; ++cube) {
+    // kg: 1-based interval index per axis, axis 0 most significant (get_indx, vegasT.cuh:136-154)
+    int kg[MAXD];
+    uint64_t q = cube;
+#pragma unroll
+    for (int j = MAXD - 1; j >= 0; --j) {
+      if (j < A.d) {
+        kg[j] = 1 + (int)(q % (uint64_t)A.ng);
+        q /= (uint64_t)A.ng;
+      }
+    }
+    double fb = 0.0, f2b = 0.0;
+    for (int k = 1; k <= A.npg; ++k) {
+      double wgt = A.xjac;
+      double x[MAXD];
+      int ia[MAXD];
+      uint32_t rnd[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int j = 0; j < MAXD; ++j) {
+        if (j < A.d) {
+          if ((j & 1) == 0) {
+            rnd[0] = (uint32_t)cube;
+            rnd[1] = (uint32_t)k | ((uint32_t)(cube >> 32) << 16);
+            rnd[2] = (uint32_t)(j >> 1);
+            rnd[3] = A.iter;
+            philox4x32_10(rnd, A.key0, A.key1);
+          }
+          const double ran = (j & 1) ? philox_unit(rnd[2], rnd[3]) : philox_unit(rnd[0], rnd[1]);
+          // Setup_Integrand_Eval (vegasT.cuh:173-212)
+          const double xn = __fma_rn(__dsub_rn((double)kg[j], ran), A.dxg, 1.0);
+          const int b = max(min((int)xn, A.nbins), 1);
+          const double* xij = sxi + j * nb1;
+          double xo, rc;
+          if (b > 1) {
+            xo = __dsub_rn(xij[b], xij[b - 1]);
+            rc = __fma_rn(__dsub_rn(xn, (double)b), xo, xij[b - 1]);
+          } else {
+            xo = xij[b];
+            rc = __dmul_rn(__dsub_rn(xn, (double)b), xo);
+          }
+          x[j] = __fma_rn(rc, A.dx[j], A.regn[j]);
+          wgt = __dmul_rn(wgt, __dmul_rn(xo, A.xnd));
+          ia[j] = b;
+        }
+      }
+      const double f = __dmul_rn(wgt, fn.template eval<MAXD>(A.desc, x));
+      const double f2 = __dmul_rn(f, f);
+      fb = __dadd_rn(fb, f);
+      f2b = __dadd_rn(f2b, f2);
+      if (A.adapt) {
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j)
+          if (j < A.d) atomicAdd(&hist[j * nb1 + ia[j]], f2);
+      }
+    }
+    // per-cube variance term (vegasT.cuh:336-343)
+    f2b = sqrt(__dmul_rn(f2b, (double)A.npg));
+    f2b = __dmul_rn(__dsub_rn(f2b, fb), __dadd_rn(f2b, fb));
+    if (f2b <= 0.0) f2b = kTiny;
+    fbg = __dadd_rn(fbg, fb);
+    f2bg = __dadd_rn(f2bg, f2b);
+  }
+  // Block sums: shuffle-down trees, then the 8 warp results in order.
+  __shared__ double red[2][8];
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    fbg = __dadd_rn(fbg, __shfl_down_sync(0xffffffffu, fbg, off));
+    f2bg = __dadd_rn(f2bg, __shfl_down_sync(0xffffffffu, f2bg, off));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = fbg;
+    red[1][warp] = f2bg;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int w = 0; w < kMcThreads / 32; ++w) {
+      s0 = __dadd_rn(s0, red[0][w]);
+      s1 = __dadd_rn(s1, red[1][w]);
+    }
+    A.partial[2 * blockIdx.x] = s0;
+    A.partial[2 * blockIdx.x + 1] = s1;
+  }
+  if (A.adapt) {
+    for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) {
+      const double v = hist[i];
+      if (v != 0.0) atomicAdd(&A.bins[i], v);
+    }
+  }
+}
+
+// Shared memory the kernel may use: the grid and the bin histogram.
+constexpr size_t kMcMaxSmem = 200 * 1024;
+
+// Host launch of one m-Cubes iteration for an integrand functor type Fn.
+template <int MAXD, class Fn>
+inline cudaError_t launch_mcubes(const pg_mcubes_args& a, const Fn& fn) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e =
+        cudaFuncSetAttribute(mcubes_kernel<MAXD, Fn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcMaxSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  mcubes_kernel<MAXD, Fn><<<kMcBlocks, kMcThreads, (size_t)a.smem, (cudaStream_t)a.stream>>>(
+      *static_cast<const McArgs*>(a.args), fn);
+  return cudaGetLastError();
+}
+
+}  // namespace pg

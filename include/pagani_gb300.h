@@ -21,7 +21,7 @@ extern "C" {
 
 #define PG_MAX_DIM 16
 #define PG_MIN_NDIM 2
-#define PG_MAX_NDIM 10
+#define PG_MAX_NDIM 12
 
 /* Return codes.  PG_NOT_CONVERGED mirrors the reference's status 1
  * (common/integration_result.hh:17); the negative codes replace the
@@ -101,14 +101,9 @@ typedef struct pg_options {
   int32_t max_iters;
   double device_mem_model;  /* bytes seen by the memory-pressure classifier */
   uint64_t max_regions;     /* hard cap of the region pool (0 = derived from the model) */
-  int32_t eval_mode;        /* 0 = exact reference order; see pg_eval_mode */
+  int32_t eval_mode;        /* must be 0: per-region rule sums in the reference's order */
   int32_t reserved;
 } pg_options;
-
-typedef enum pg_eval_mode {
-  PG_EVAL_REFERENCE_ORDER = 0, /* per-region sums in the reference's exact order */
-  PG_EVAL_FACTORED = 1         /* separable families: per-axis factors computed once per region */
-} pg_eval_mode;
 
 typedef struct pg_context pg_context;
 
@@ -123,6 +118,9 @@ typedef struct pg_stats {
   uint64_t stage_bytes;      /* algorithmic bytes moved by those stages */
   uint64_t h2d_bytes;
   uint64_t d2h_bytes;
+  int32_t tune_warps[2];        /* autotuned regions per block: [0] ndim <= 8, [1] ndim > 8 */
+  int32_t tune_ctas_per_sm[2];  /* autotuned grid cap (blocks per SM) of the evaluation kernel */
+  uint64_t eval_bytes;          /* algorithmic HBM bytes of the evaluation launches */
 } pg_stats;
 
 void pg_options_default(pg_options* opt);
@@ -153,12 +151,55 @@ int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double e
  * stage tests call directly (test/cuda/pagani/RegionSampling.cu:48-88). */
 int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,
                         uint64_t n, const double* left, const double* length, double* est, double* err,
-                        int32_t* bisect, int32_t eval_mode);
+                        int32_t* bisect, int32_t eval_mode /* must be 0 */);
 
 /* Same on device buffers, asynchronous on the context stream. */
 int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,
                                uint64_t n, const double* d_left, const double* d_length, double* d_est,
                                double* d_err, int32_t* d_bisect, int32_t eval_mode);
+
+/* ---------------- user integrands (C++ layer) ----------------
+ * A device functor cannot cross a C ABI, but a caller compiled with nvcc can
+ * instantiate the region-evaluation kernel for its own functor and give the
+ * library a launcher for it.  include/pagani_gb300.cuh does this for
+ * Workspace<T,ndim>::integrate(f, epsrel, epsabs, vol, relerr_classification)
+ * (cuda/pagani/quad/GPUquad/Workspace.cuh:52-70), whose integrands are any
+ * copyable type with a __device__ operator() of ndim doubles
+ * (common/cuda/cudaApply.cuh:7-26).  The library runs the whole iteration and
+ * calls launch(args, user) once per evaluation launch; args point at the
+ * library's device buffers, `descs` and `rule` are opaque to C, and launch
+ * returns 0 or a cudaError_t value. */
+typedef struct pg_eval_args {
+  const double* left;    /* SoA region list, coordinate k of region i at [k * stride + i] */
+  const double* length;
+  uint64_t n;            /* regions */
+  uint64_t stride;
+  const uint32_t* owner; /* integral of each region, NULL when the list holds one integral */
+  const void* descs;     /* device array of the library's per-integral descriptors */
+  const void* rule;      /* host pointer to the library's rule-table block (device pointers inside) */
+  double* est;
+  double* err;
+  int32_t* bisect;
+  int32_t maxd;          /* largest ndim in the list */
+  int32_t num_sms;
+  void* stream;          /* cudaStream_t to launch on */
+  int32_t warps;         /* autotuned regions per block: 4 or 8 */
+  int32_t ctas_per_sm;   /* autotuned grid cap */
+} pg_eval_args;
+
+typedef int (*pg_eval_launcher)(const pg_eval_args* args, void* user);
+
+/* pg_integrate for a user integrand of ndim dimensions evaluated by `launch`. */
+int pg_integrate_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user, double epsrel,
+                          double epsabs, const double* lows, const double* highs, const pg_options* opt,
+                          pg_result* out);
+
+/* pg_evaluate_regions for a user integrand (host buffers, SoA [dim * n + i]):
+ * the region-evaluation stage test (test/cuda/pagani/RegionSampling.cu:48-88)
+ * for functors. */
+int pg_evaluate_regions_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user,
+                                 const double* lows, const double* highs, uint64_t n, const double* left,
+                                 const double* length, double* est, double* err, int32_t* bisect);
 
 /* Two-level error estimate and relative-error classification on host buffers.
  * Replaces two_level_errorest_and_relerr_classify / RefineError
@@ -215,6 +256,25 @@ typedef struct pg_mcubes_options {
 void pg_mcubes_options_default(pg_mcubes_options* opt);
 int pg_mcubes_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double epsabs, const double* lows,
                         const double* highs, const pg_mcubes_options* opt, pg_result* out);
+
+/* m-Cubes for a user integrand (C++ layer: cuda_mcubes::integrate<F, NDIM> in
+ * include/pagani_gb300.cuh): launch(args, user) runs one sampling iteration
+ * of the library's m-Cubes kernel instantiated for the caller's functor;
+ * `args` is the kernel's argument block (opaque to C), launch returns 0 or a
+ * cudaError_t value. */
+typedef struct pg_mcubes_args {
+  const void* args; /* kernel argument block */
+  uint64_t smem;    /* dynamic shared memory bytes */
+  void* stream;     /* cudaStream_t */
+  int32_t maxd;     /* ndim */
+  int32_t pad;
+} pg_mcubes_args;
+
+typedef int (*pg_mcubes_launcher)(const pg_mcubes_args* args, void* user);
+
+int pg_mcubes_integrate_launcher(pg_context* ctx, int32_t ndim, pg_mcubes_launcher launch, void* user,
+                                 double epsrel, double epsabs, const double* lows, const double* highs,
+                                 const pg_mcubes_options* opt, pg_result* out);
 
 /* ---------------- batched PAGANI ----------------
  * Integrates `count` independent integrands (any mix of ndim, family and
