@@ -148,10 +148,11 @@ Engine::~Engine() {
   DevBuf* dev_bufs[] = {&rule_trie_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
                         &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
                         &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
-                        &thr_out_};
+                        &thr_out_, &adm_starts_, &adm_ids_, &sp_left_, &sp_len_, &sp_par_};
   for (DevBuf* b : dev_bufs)
     if (b->p) cudaFree(b->p);
-  DevBuf* host_bufs[] = {&h_segs_, &h_chunks_, &h_trans_, &h_scal_, &h_live_, &h_thr_};
+  DevBuf* host_bufs[] = {&h_segs_, &h_chunks_, &h_trans_, &h_trans_spill_, &h_scal_, &h_live_, &h_thr_,
+                         &h_adm_starts_, &h_adm_ids_};
   for (DevBuf* b : host_bufs)
     if (b->p) cudaFreeHost(b->p);
   for (auto& e : ev_)
@@ -170,6 +171,68 @@ int Engine::fail(cudaError_t e, const char* what) {
     cudaError_t e_ = (call);                \
     if (e_ != cudaSuccess) return fail(e_, what); \
   } while (0)
+
+SpillArena::~SpillArena() {
+  for (Block& b : blocks_) cudaFreeHost(b.base);
+}
+
+void* SpillArena::alloc(size_t bytes) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (bytes == 0) bytes = 256;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    for (Block& b : blocks_)
+      for (auto it = b.free.begin(); it != b.free.end(); ++it)
+        if (it->second >= bytes) {
+          const size_t off = it->first, len = it->second;
+          b.free.erase(it);
+          if (len > bytes) b.free[off + bytes] = len - bytes;
+          return b.base + off;
+        }
+    // No room: a new block of at least 1 GiB.
+    const size_t want = std::max(bytes, (size_t)1 << 30);
+    void* p = nullptr;
+    if (cudaMallocHost(&p, want) != cudaSuccess) return nullptr;
+    Block nb;
+    nb.base = (char*)p;
+    nb.bytes = want;
+    nb.free[0] = want;
+    blocks_.push_back(std::move(nb));
+    total_ += want;
+  }
+  return nullptr;
+}
+
+void SpillArena::release(void* ptr, size_t bytes) {
+  if (!ptr) return;
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (bytes == 0) bytes = 256;
+  char* p = (char*)ptr;
+  for (Block& b : blocks_) {
+    if (p < b.base || p >= b.base + b.bytes) continue;
+    size_t off = (size_t)(p - b.base), len = bytes;
+    auto next = b.free.lower_bound(off);
+    if (next != b.free.end() && off + len == next->first) {  // merge with the following range
+      len += next->second;
+      next = b.free.erase(next);
+    }
+    if (next != b.free.begin()) {  // merge with the preceding range
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        prev->second += len;
+        return;
+      }
+    }
+    b.free[off] = len;
+    return;
+  }
+}
+
+void SpillArena::reset() {
+  for (Block& b : blocks_) {
+    b.free.clear();
+    b.free[0] = b.bytes;
+  }
+}
 
 int Engine::ensure(DevBuf& b, size_t bytes) {
   if (b.bytes >= bytes) return PG_OK;
@@ -240,6 +303,7 @@ int Engine::init(std::string* why) {
   }
   const double q = r2.G[1] / r2.G[0];
   R.ratio = q * q;
+  R.omr = 1.0 - R.ratio;
   if ((rc = ensure(rule_code_, codes.size() * 8)) != PG_OK) {
     if (why) *why = last_error;
     return rc;
@@ -514,6 +578,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   if ((rc = ensure(adm_ids_, (njobs + 1) * sizeof(uint32_t))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_segs_, njobs * sizeof(SegDesc))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_trans_, njobs * sizeof(Transition))) != PG_OK) return rc;
+  if ((rc = ensure_pinned(h_trans_spill_, njobs * sizeof(Transition))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_scal_, njobs * sizeof(IterScalars))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_live_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
   if ((rc = ensure_pinned(h_adm_starts_, (njobs + 1) * sizeof(uint64_t))) != PG_OK) return rc;
@@ -543,10 +608,10 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     J.iters = 0;
     J.done = false;
     J.state = JOB_PENDING;
-    J.sp_left.clear();
-    J.sp_len.clear();
-    J.sp_par.clear();
+    J.sp = nullptr;
+    J.sp_bytes = 0;
   }
+  spill_.reset();
   const auto t_start = std::chrono::steady_clock::now();
   int cur = 0;
   uint64_t T = 0, P = 0;  // regions and parent estimates in the current list
@@ -613,21 +678,25 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
         for (uint32_t j : restore) {
           Job& J = jobs[j];
           const int d = J.desc.d;
-          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, J.sp_left.data(), J.n * 8,
-                                   J.n * 8, d, cudaMemcpyHostToDevice, stream_), "restore");
-          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, J.sp_len.data(), J.n * 8,
-                                   J.n * 8, d, cudaMemcpyHostToDevice, stream_), "restore");
-          PG_TRY(cudaMemcpyAsync((double*)parent_[cur].p + J.par_start, J.sp_par.data(), (J.n / 2) * 8,
-                                 cudaMemcpyHostToDevice, stream_), "restore");
+          const double* sl = J.sp;
+          const double* sn = J.sp + J.n * d;
+          const double* sq = J.sp + 2 * J.n * d;
+          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, sl, J.n * 8, J.n * 8, d,
+                                   cudaMemcpyHostToDevice, stream_), "restore");
+          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, sn, J.n * 8, J.n * 8, d,
+                                   cudaMemcpyHostToDevice, stream_), "restore");
+          PG_TRY(cudaMemcpyAsync((double*)parent_[cur].p + J.par_start, sq, (J.n / 2) * 8, cudaMemcpyHostToDevice,
+                                 stream_), "restore");
           fill_owner_kernel<<<(unsigned)div_up(J.n, 256), 256, 0, stream_>>>((uint32_t*)owner_[cur].p, J.start, J.n,
                                                                             j);
           stats.launches++;
           PG_TRY(cudaGetLastError(), "restore launch");
           stats.h2d_bytes += J.n * 16 * d + J.n * 4;
-          PG_TRY(cudaStreamSynchronize(stream_), "restore");  // host copies may be released now
-          std::vector<double>().swap(J.sp_left);
-          std::vector<double>().swap(J.sp_len);
-          std::vector<double>().swap(J.sp_par);
+          // The slice may be handed out again at once: its next writer is a
+          // copy queued behind these on the same stream.
+          spill_.release(J.sp, J.sp_bytes);
+          J.sp = nullptr;
+          J.sp_bytes = 0;
         }
         T = t;
         P = pp;
@@ -834,10 +903,28 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       }
       ht[j] = Tr;
     }
-    PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
-           "transition upload");
-    stats.h2d_bytes += njobs * sizeof(Transition);
-    // Spilled integrals: children into a transient buffer, then to host memory.
+    // Spilled integrals: each one's children go to offset 0 of a transient
+    // device buffer (one compaction per integral) and from there to pinned
+    // host memory; then every spilled integral is excluded (mode 0) from the
+    // compaction of the resident list.  The two transition tables are
+    // separate pinned arrays that the host does not touch again before the
+    // end-of-iteration synchronisation, so no copy here needs a host wait.
+    Transition* hsp = (Transition*)h_trans_spill_.p;
+    if (!spill.empty()) {
+      std::memcpy(hsp, ht, njobs * sizeof(Transition));
+      for (uint32_t j : spill) {
+        hsp[j].out_start = 0;
+        hsp[j].par_out = 0;
+        ht[j].mode = 0;
+      }
+      PG_TRY(cudaMemcpyAsync(trans_.p, hsp, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
+             "transition upload");
+      stats.h2d_bytes += njobs * sizeof(Transition);
+    } else {
+      PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
+             "transition upload");
+      stats.h2d_bytes += njobs * sizeof(Transition);
+    }
     for (uint32_t j : spill) {
       Job& J = jobs[j];
       const SegDesc& S = hs[j];
@@ -846,31 +933,28 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       if ((rc = ensure(sp_left_, n2 * maxd * 8)) != PG_OK) return rc;
       if ((rc = ensure(sp_len_, n2 * maxd * 8)) != PG_OK) return rc;
       if ((rc = ensure(sp_par_, A * 8)) != PG_OK) return rc;
-      // This job's transition must place it at offset 0 of the transient buffer.
-      Transition Tr = ht[j];
-      Tr.out_start = 0;
-      Tr.par_out = 0;
-      PG_TRY(cudaMemcpyAsync((Transition*)trans_.p + j, &Tr, sizeof Tr, cudaMemcpyHostToDevice, stream_),
-             "transition upload");
       if ((rc = compact(cur, cur ^ 1, S.chunk_start, S.nchunks, maxd, (double*)sp_left_.p, (double*)sp_len_.p, n2,
                         nullptr, (double*)sp_par_.p)) != PG_OK)
         return rc;
-      J.sp_left.resize(n2 * d);
-      J.sp_len.resize(n2 * d);
-      J.sp_par.resize(A);
-      PG_TRY(cudaMemcpyAsync(J.sp_left.data(), sp_left_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-      PG_TRY(cudaMemcpyAsync(J.sp_len.data(), sp_len_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-      PG_TRY(cudaMemcpyAsync(J.sp_par.data(), sp_par_.p, A * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-      PG_TRY(cudaStreamSynchronize(stream_), "spill");
+      J.sp_bytes = (2 * n2 * d + A) * 8;
+      J.sp = (double*)spill_.alloc(J.sp_bytes);
+      if (!J.sp) {
+        last_error = "pinned host memory for a spilled region list";
+        return PG_OOM;
+      }
+      // The transient buffer's rows are n2 apart; the slice keeps them packed.
+      PG_TRY(cudaMemcpyAsync(J.sp, sp_left_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+      PG_TRY(cudaMemcpyAsync(J.sp + n2 * d, sp_len_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+      PG_TRY(cudaMemcpyAsync(J.sp + 2 * n2 * d, sp_par_.p, A * 8, cudaMemcpyDeviceToHost, stream_), "spill");
       stats.d2h_bytes += n2 * d * 16 + A * 8;
-      Tr.mode = 0;  // not part of the resident compaction below
-      ht[j] = Tr;
-      PG_TRY(cudaMemcpyAsync((Transition*)trans_.p + j, &ht[j], sizeof Tr, cudaMemcpyHostToDevice, stream_),
-             "transition upload");
-      PG_TRY(cudaStreamSynchronize(stream_), "transition upload");
       J.state = JOB_SPILLED;
       J.n = n2;
       J.has_parent = 1;
+    }
+    if (!spill.empty()) {
+      PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
+             "transition upload");
+      stats.h2d_bytes += njobs * sizeof(Transition);
     }
     const int nxt = cur ^ 1;
     if (out_total > 0) {

@@ -11,6 +11,7 @@
 #include <stdint.h>
 
 #include <functional>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -111,9 +112,37 @@ struct Job {
   int error = 0;
   int state = JOB_PENDING;
   double done_ms = 0.0;  // host time from the start of the run to the iteration that finished it
-  // Next region list of a job moved out of the device pool (host copy):
-  // rows [dim][n] of left and length, and the n/2 parent estimates.
-  std::vector<double> sp_left, sp_len, sp_par;
+  // Next region list of a job moved out of the device pool, in the engine's
+  // pinned spill arena: rows [dim][n] of left, then of length, then the n/2
+  // parent estimates.
+  double* sp = nullptr;
+  size_t sp_bytes = 0;
+};
+
+// Pinned host storage for region lists moved out of the device pool.  Blocks
+// of page-locked memory are allocated as needed and kept for the engine's
+// lifetime; slices are handed out first-fit.  Every access to a slice is a
+// copy on the engine's stream, so reusing a slice needs no host
+// synchronisation.
+class SpillArena {
+ public:
+  ~SpillArena();
+  // A slice of at least `bytes` (256-byte aligned), or nullptr when pinned
+  // memory cannot be had.
+  void* alloc(size_t bytes);
+  void release(void* p, size_t bytes);
+  // Marks every block free (no job of a finished run still holds a slice).
+  void reset();
+  size_t pinned_bytes() const { return total_; }
+
+ private:
+  struct Block {
+    char* base;
+    size_t bytes;
+    std::map<size_t, size_t> free;  // offset -> length
+  };
+  std::vector<Block> blocks_;
+  size_t total_ = 0;
 };
 
 // Scheduling limits of one run.
@@ -198,9 +227,10 @@ class Engine {
   DevBuf segs_, trans_, descs_, scal_, live_, thr_out_, adm_starts_, adm_ids_;
   // transient device copy of one job's next list on its way to host memory
   DevBuf sp_left_, sp_len_, sp_par_;
+  SpillArena spill_;
   bool compact_timing_pending_ = false;
   // pinned host mirrors
-  DevBuf h_segs_, h_chunks_, h_trans_, h_scal_, h_live_, h_thr_, h_adm_starts_, h_adm_ids_;
+  DevBuf h_segs_, h_chunks_, h_trans_, h_trans_spill_, h_scal_, h_live_, h_thr_, h_adm_starts_, h_adm_ids_;
   cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 

@@ -29,6 +29,7 @@ struct RuleDev {
   double A[kCodesPerDim];           // .5 + g for the 11 coordinate codes
   double B[kCodesPerDim];           // .5 - g
   double ratio;                     // (G1 / G0)^2 of the fourth difference (Sample.cuh:195-196)
+  double omr;                       // 1 - ratio
 };
 
 // ---------------------------------------------------------------------------
@@ -66,6 +67,70 @@ struct EvalWarpSmem {
   double scale[kNSets * kNRules];
   double norm[kNSets * kNRules];
 };
+
+// Rule sums of one region: virtual thread l (lane l) in a*, virtual thread
+// l + 32 in b*, rules 0..4.
+struct RuleSums {
+  double a0, a1, a2, a3, a4, b0, b1, b2, b3, b4;
+};
+
+// How a point's value is formed: from the prefix trie of per-axis factors
+// (product-form integrands, d <= 8), as the left-to-right product of per-axis
+// factors, or by evaluating the integrand on the point's coordinates.
+constexpr int kPointsTrie = 0, kPointsProduct = 1, kPointsEval = 2;
+
+// The per-point loop of eval_kernel: lane l takes points l, l+64, ... into a*
+// and l+32, l+96, ... into b*, in ascending order, with fused multiply-adds,
+// as the reference's threads l and l+32 do (Sample.cuh:221-259).  f is
+// multiplied by the box's Jacobian when SCALE (Sample.cuh:236).  The first 64
+// values are kept in S.fv for the fourth differences.
+template <int MAXD, int MODE, bool SCALE, class Fn>
+__device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, const Fn& fn,
+                                           const uint64_t* __restrict__ codes, int feval, int d, int lane,
+                                           const uint16_t* __restrict__ leaf_tab, const double* leaf_src,
+                                           const double* leaf_fac, double jac) {
+  for (int base = 0; base < feval; base += 64) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int p = base + half * 32 + lane;
+      if (p < feval) {
+        const uint64_t code = __ldg(&codes[p]);
+        double f;
+        if constexpr (MODE == kPointsTrie) {
+          const uint32_t e = __ldg(&leaf_tab[p]);
+          f = __dmul_rn(leaf_src[e & 0xfffu], leaf_fac[e >> 12]);
+        } else if constexpr (MODE == kPointsProduct) {
+          f = S.fac[(int)(code & 15u)];
+#pragma unroll
+          for (int k = 1; k < MAXD; ++k)
+            if (k < d) f = __dmul_rn(f, S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)]);
+        } else {
+          double x[MAXD];
+#pragma unroll
+          for (int k = 0; k < MAXD; ++k)
+            x[k] = (k < d) ? S.tab[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)] : 0.0;
+          f = fn.template eval<MAXD>(S.desc, x);
+        }
+        if constexpr (SCALE) f = __dmul_rn(f, jac);
+        if (base == 0) S.fv[p] = f;
+        const double* w = &S.w[(int)(code >> 60) * kNRules];
+        if (half == 0) {
+          rs.a0 = __fma_rn(f, w[0], rs.a0);
+          rs.a1 = __fma_rn(f, w[1], rs.a1);
+          rs.a2 = __fma_rn(f, w[2], rs.a2);
+          rs.a3 = __fma_rn(f, w[3], rs.a3);
+          rs.a4 = __fma_rn(f, w[4], rs.a4);
+        } else {
+          rs.b0 = __fma_rn(f, w[0], rs.b0);
+          rs.b1 = __fma_rn(f, w[1], rs.b1);
+          rs.b2 = __fma_rn(f, w[2], rs.b2);
+          rs.b3 = __fma_rn(f, w[3], rs.b3);
+          rs.b4 = __fma_rn(f, w[4], rs.b4);
+        }
+      }
+    }
+  }
+}
 
 template <int MAXD, int WARPS, class Fn>
 static __global__ void __launch_bounds__(WARPS * 32)
@@ -143,50 +208,26 @@ static __global__ void __launch_bounds__(WARPS * 32)
       }
     }
     const double* leaf_fac = S.fac + (d - 1) * kCodesPerDim;
+    // The per-point loop, specialised on how f is formed and on whether the
+    // box's Jacobian differs from 1 (both uniform over the region), so no
+    // per-point instruction is spent on either decision.
     const double jac = S.desc.jac;
-    const bool scale = jac != 1.0;
-    double sa0 = 0, sa1 = 0, sa2 = 0, sa3 = 0, sa4 = 0;
-    double sb0 = 0, sb1 = 0, sb2 = 0, sb3 = 0, sb4 = 0;
-    for (int base = 0; base < feval; base += 64) {
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int p = base + half * 32 + lane;
-        if (p < feval) {
-          const uint64_t code = __ldg(&codes[p]);
-          double f;
-          if (sep && leaf_tab) {
-            const uint32_t e = __ldg(&leaf_tab[p]);
-            f = __dmul_rn(leaf_src[e & 0xfffu], leaf_fac[e >> 12]);
-          } else if (sep) {
-            f = S.fac[(int)(code & 15u)];
-#pragma unroll
-            for (int k = 1; k < MAXD; ++k)
-              if (k < d) f = __dmul_rn(f, S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)]);
-          } else {
-            double x[MAXD];
-#pragma unroll
-            for (int k = 0; k < MAXD; ++k)
-              x[k] = (k < d) ? S.tab[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)] : 0.0;
-            f = fn.template eval<MAXD>(S.desc, x);
-          }
-          if (scale) f = __dmul_rn(f, jac);
-          if (base == 0) S.fv[p] = f;
-          const double* w = &S.w[(int)(code >> 60) * kNRules];
-          if (half == 0) {
-            sa0 = __fma_rn(f, w[0], sa0);
-            sa1 = __fma_rn(f, w[1], sa1);
-            sa2 = __fma_rn(f, w[2], sa2);
-            sa3 = __fma_rn(f, w[3], sa3);
-            sa4 = __fma_rn(f, w[4], sa4);
-          } else {
-            sb0 = __fma_rn(f, w[0], sb0);
-            sb1 = __fma_rn(f, w[1], sb1);
-            sb2 = __fma_rn(f, w[2], sb2);
-            sb3 = __fma_rn(f, w[3], sb3);
-            sb4 = __fma_rn(f, w[4], sb4);
-          }
-        }
-      }
+    RuleSums rs{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int mode = (sep && leaf_tab) ? kPointsTrie : (sep ? kPointsProduct : kPointsEval);
+    if (jac != 1.0) {
+      if (mode == kPointsTrie)
+        point_sums<MAXD, kPointsTrie, true>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+      else if (mode == kPointsProduct)
+        point_sums<MAXD, kPointsProduct, true>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+      else
+        point_sums<MAXD, kPointsEval, true>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+    } else {
+      if (mode == kPointsTrie)
+        point_sums<MAXD, kPointsTrie, false>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+      else if (mode == kPointsProduct)
+        point_sums<MAXD, kPointsProduct, false>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+      else
+        point_sums<MAXD, kPointsEval, false>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
     }
     // The reference's block sum (Sample.cuh:49-83) per rule: a shuffle-down
     // tree over each 32-lane half (offsets 16, 8, 4, 2, 1), then
@@ -199,16 +240,16 @@ static __global__ void __launch_bounds__(WARPS * 32)
     else
       red = S.tab;
     __syncwarp();
-    red[0 * 32 + lane] = sa0;
-    red[1 * 32 + lane] = sa1;
-    red[2 * 32 + lane] = sa2;
-    red[3 * 32 + lane] = sa3;
-    red[4 * 32 + lane] = sa4;
-    red[5 * 32 + lane] = sb0;
-    red[6 * 32 + lane] = sb1;
-    red[7 * 32 + lane] = sb2;
-    red[8 * 32 + lane] = sb3;
-    red[9 * 32 + lane] = sb4;
+    red[0 * 32 + lane] = rs.a0;
+    red[1 * 32 + lane] = rs.a1;
+    red[2 * 32 + lane] = rs.a2;
+    red[3 * 32 + lane] = rs.a3;
+    red[4 * 32 + lane] = rs.a4;
+    red[5 * 32 + lane] = rs.b0;
+    red[6 * 32 + lane] = rs.b1;
+    red[7 * 32 + lane] = rs.b2;
+    red[8 * 32 + lane] = rs.b3;
+    red[9 * 32 + lane] = rs.b4;
     __syncwarp();
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
@@ -223,64 +264,125 @@ static __global__ void __launch_bounds__(WARPS * 32)
     const double s0 = red[320], s1 = red[321], s2 = red[322], s3 = red[323], s4 = red[324];
     __syncwarp();
 
-    // base + ratio*(fp+fm) - (fp2+fm2): the reference's compiled code fuses
-    // the multiply of base (2*f0*(1-ratio)) for d <= 4 and the multiply
-    // ratio*(fp+fm) for d >= 5 (pinned against the reference kernel's output).
-    double key = -1.0;
+    // Fourth difference per axis k: base + ratio*(fp+fm) - (fp2+fm2) with
+    // base = 2*f0*(1-ratio) (Sample.cuh:190-215).  The reference's compiled
+    // code fuses the base multiply for d <= 4 and the ratio multiply for
+    // d >= 5 (pinned against the reference kernel's output).  The three sums
+    // share one warp addition: lanes 0..d-1 form fp+fm, lanes d..2d-1 form
+    // fp2+fm2 of axis lane-d, lane 31 forms f0+f0 = 2*f0.
+    //
+    // The split-axis search and the null-rule maxima below are maxima of
+    // non-negative doubles, taken on their bit patterns (for non-negative
+    // doubles the integer order is the numeric order) so they stay off the
+    // FP64 pipe.  A bit pattern of 0 means "no candidate".
+    double ua = 0.0, ub = 0.0;
     if (lane < d) {
-      const double f02 = __dmul_rn(S.fv[0], 2.0), omr = __dsub_rn(1.0, rule.ratio);
-      const double fp = S.fv[1 + 2 * lane], fm = S.fv[2 + 2 * lane];
-      const double fp2 = S.fv[1 + 2 * lane + 2 * d], fm2 = S.fv[2 + 2 * lane + 2 * d];
-      const double X = __dadd_rn(fp, fm);
-      const double s = (d <= 4) ? __fma_rn(f02, omr, __dmul_rn(rule.ratio, X))
-                                : __fma_rn(rule.ratio, X, __dmul_rn(f02, omr));
-      const double fd = fabs(__dsub_rn(s, __dadd_rn(fp2, fm2)));
-      if (fd > 0.0) key = fd;
+      ua = S.fv[1 + 2 * lane];
+      ub = S.fv[2 + 2 * lane];
+    } else if (lane < 2 * d) {
+      ua = S.fv[1 + 2 * (lane - d) + 2 * d];
+      ub = S.fv[2 + 2 * (lane - d) + 2 * d];
+    } else if (lane == 31) {
+      ua = ub = S.fv[0];
     }
-    double kmax = key;
+    const double sums = __dadd_rn(ua, ub);
+    const double fsec = __shfl_sync(full, sums, (lane + d) & 31);  // fp2 + fm2 of this lane's axis
+    const double f02 = __shfl_sync(full, sums, 31);
+    unsigned long long key = 0;
+    if (lane < d) {
+      const double X = sums;
+      const double s = (d <= 4) ? __fma_rn(f02, rule.omr, __dmul_rn(rule.ratio, X))
+                                : __fma_rn(rule.ratio, X, __dmul_rn(f02, rule.omr));
+      const unsigned long long fd = (unsigned long long)__double_as_longlong(fabs(__dsub_rn(s, fsec)));
+      if (fd != 0ull && fd <= 0x7ff0000000000000ull) key = fd;  // fd > 0 (a NaN is no candidate)
+    }
+    unsigned long long kmax = key;
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) kmax = fmax(kmax, __shfl_xor_sync(full, kmax, off));
-    int cand = (kmax > 0.0 && key == kmax) ? lane : 64;
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) cand = min(cand, __shfl_xor_sync(full, cand, off));
+    for (int off = 16; off >= 1; off >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(full, kmax, off);
+      kmax = o > kmax ? o : kmax;
+    }
+    const unsigned cmask = __ballot_sync(full, kmax != 0ull && key == kmax);
+    const int cand = cmask ? __ffs(cmask) - 1 : 64;
 
     // Null-rule error (Sample.cuh:261-289): lanes 0..26 evaluate the 27
     // (rule, set) terms, lanes 0..2 take the maximum per rule.
-    double term = 0.0;
+    // The terms are >= 0 (the null-rule norms are >= 0); a NaN term is
+    // ignored, as the reference's max() does.
+    unsigned long long term = 0;
     if (lane < 27) {
       const int q = 1 + lane / 9, s = lane - (q - 1) * 9;
       const double sq = (q == 1) ? s1 : (q == 2) ? s2 : s3;
       const double sq1 = (q == 1) ? s2 : (q == 2) ? s3 : s4;
-      term = __dmul_rn(fabs(__fma_rn(S.scale[s * kNRules + q], sq, sq1)), S.norm[s * kNRules + q]);
+      const unsigned long long b = (unsigned long long)__double_as_longlong(
+          __dmul_rn(fabs(__fma_rn(S.scale[s * kNRules + q], sq, sq1)), S.norm[s * kNRules + q]));
+      term = (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : b;
     }
-    double m = 0.0;
+    unsigned long long m = 0;
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
-      const double o = __shfl_sync(full, term, (lane < 3 ? lane : 0) * 9 + s);
-      m = fmax(m, o);
+      const unsigned long long o = __shfl_sync(full, term, (lane < 3 ? lane : 0) * 9 + s);
+      m = o > m ? o : m;
     }
-    const double e1 = __shfl_sync(full, m, 0), e2 = __shfl_sync(full, m, 1), e3 = __shfl_sync(full, m, 2);
-    // Region volume and widest axis (Phases.cuh:329-348): the side lengths in
-    // parallel, the product in axis order (1.0 * r0 = r0), and the widest-axis
-    // comparison on the bit patterns (side lengths are non-negative).
-    if (lane < d) S.up[lane] = __dsub_rn(S.up[lane], S.lo[lane]);
-    __syncwarp();
-    if (lane == 0) {
-      double vol = S.up[0];
-      long long maxbits = __double_as_longlong(vol);
-      int maxdim = 0;
-      for (int k = 1; k < d; ++k) {
-        const double rk = S.up[k];
-        vol = __dmul_rn(vol, rk);
-        const long long b = __double_as_longlong(rk);
-        if (b > maxbits) {
-          maxdim = k;
-          maxbits = b;
-        }
+    const unsigned long long m1 = __shfl_sync(full, m, 0), m2 = __shfl_sync(full, m, 1), m3 = __shfl_sync(full, m, 2);
+    const double e1 = __longlong_as_double((long long)m1), e2 = __longlong_as_double((long long)m2),
+                 e3 = __longlong_as_double((long long)m3);
+    unsigned long long mmax = m1 > m2 ? m1 : m2;
+    mmax = m3 > mmax ? m3 : mmax;
+    const double emax = __longlong_as_double((long long)mmax);
+
+    // Side lengths, widest axis and volume (Phases.cuh:329-348).  The volume
+    // is the product of the side lengths in axis order.  When every side is a
+    // power of two no larger than 1 (regions made by uniform splits and
+    // bisections in unit coordinates always are) and the product stays
+    // normal, every partial product is exact and the volume is 2^(sum of
+    // exponents), formed on the integer pipe; otherwise lane 0 multiplies in
+    // order.  The widest axis is the first one whose length exceeds all
+    // earlier ones, starting from 0 (a negative or NaN length never wins),
+    // compared on bit patterns.
+    unsigned long long sb = 0, sk = 0;
+    int expo = 0;
+    bool pow2 = true;
+    if (lane < d) {
+      const double side = __dsub_rn(S.up[lane], S.lo[lane]);
+      S.up[lane] = side;
+      sb = (unsigned long long)__double_as_longlong(side);
+      const int e = (int)((sb >> 52) & 0x7ffull);
+      pow2 = (sb & 0x800fffffffffffffull) == 0ull && e >= 1 && e <= 1023;
+      expo = e - 1023;
+      sk = ((sb >> 63) || (sb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) ? 0ull : sb;
+    }
+    const unsigned hi_max = __reduce_max_sync(full, (unsigned)(sk >> 32));
+    const unsigned lo_max = __reduce_max_sync(full, (unsigned)(sk >> 32) == hi_max ? (unsigned)sk : 0u);
+    const unsigned wmask = __ballot_sync(full, lane < d && (unsigned)(sk >> 32) == hi_max && (unsigned)sk == lo_max);
+    const int maxdim = __ffs(wmask) - 1;
+    const bool all_pow2 = __all_sync(full, pow2);
+    const int esum = __reduce_add_sync(full, expo);
+    double vol;
+    if (all_pow2 && esum >= -1022) {
+      vol = __longlong_as_double((long long)(esum + 1023) << 52);
+    } else {
+      __syncwarp();
+      double v = 0.0;
+      if (lane == 0) {
+        v = S.up[0];
+        for (int k = 1; k < d; ++k) v = __dmul_rn(v, S.up[k]);
       }
-      est[r] = __dmul_rn(vol, s0);
-      const bool ladder = (__dmul_rn(5.0, e1) <= e2) && (__dmul_rn(5.0, e2) <= e3);
-      err[r] = __dmul_rn(vol, ladder ? e1 : __dmul_rn(5.0, fmax(fmax(e1, e2), e3)));
+      vol = __shfl_sync(full, v, 0);
+    }
+    // One multiply for vol*s0 (lane 0) and 5*e1, 5*e2, 5*max (lanes 1..3), one
+    // compare for the error ladder 5*e1 <= e2, 5*e2 <= e3 (lanes 1, 2), one
+    // multiply for the error (Sample.cuh:284-289).
+    const double pa = (lane == 0) ? vol : 5.0;
+    const double pb = (lane == 0) ? s0 : (lane == 1) ? e1 : (lane == 2) ? e2 : emax;
+    const double prod = __dmul_rn(pa, pb);
+    const bool le = prod <= ((lane == 1) ? e2 : e3);
+    const unsigned lmask = __ballot_sync(full, le);
+    const bool ladder = ((lmask >> 1) & 3u) == 3u;
+    const double five_max = __shfl_sync(full, prod, 3);
+    if (lane == 0) {
+      est[r] = prod;
+      err[r] = __dmul_rn(vol, ladder ? e1 : five_max);
       bisect[r] = (cand < 64) ? cand : maxdim;
     }
     __syncwarp();

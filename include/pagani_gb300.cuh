@@ -25,9 +25,10 @@
  * Build: nvcc -std=c++17 -gencode arch=compute_103a,code=sm_103a -cudart shared
  *        -I<repo>/include app.cu -L<repo>/gpuintegration_gb300 -lpagani_gb300
  *
- * The reference's names (::Workspace, quad::Volume, numint::integration_result)
- * are declared as aliases of the pagani:: ones unless
- * PAGANI_GB300_NO_REFERENCE_NAMES is defined before inclusion.
+ * ::Workspace, cuda_mcubes:: and quad::mcubes are declared as aliases of the
+ * pagani:: implementations unless PAGANI_GB300_NO_REFERENCE_NAMES is defined
+ * before inclusion (do not include the reference's Workspace.cuh or
+ * vegasT.cuh with this header: they are what it replaces).
  */
 #ifndef PAGANI_GB300_CUH
 #define PAGANI_GB300_CUH
@@ -48,10 +49,16 @@
 #include "../gpuintegration_gb300/csrc/pg_eval.cuh"
 #include "../gpuintegration_gb300/csrc/pg_mcubes_kernel.cuh"
 
-namespace pagani {
-
-// numint::integration_result (common/integration_result.hh:11-21); neval is
-// filled (regions evaluated x points per region).
+// numint::integration_result (common/integration_result.hh:11-21) and
+// quad::Volume (common/cuda/Volume.cuh:9-52) are declared under the
+// reference headers' own include guards, with the same members, so that the
+// reference's integrand-side headers (Interp1D/2D/3D, cudaArray, ...), which
+// include them, can be used inside functors together with this header, in
+// either include order.
+#ifndef GPUINTEGRATION_COMMON_INTEGRATION_RESULT_H
+#define GPUINTEGRATION_COMMON_INTEGRATION_RESULT_H
+namespace numint {
+// neval is filled here (regions evaluated x points per region).
 struct integration_result {
   double estimate = 0.;
   double errorest = 0.;
@@ -68,31 +75,46 @@ inline std::ostream& operator<<(std::ostream& os, integration_result const& res)
   os << res.estimate << "," << res.errorest << "," << res.nregions << "," << res.chi_sq << "," << res.status;
   return os;
 }
+}  // namespace numint
+#endif
 
-// quad::Volume (common/cuda/Volume.cuh:9-52): the integration box.
+#ifndef CUDACUHRE_QUAD_GPUQUAD_VOLUME_CUH
+#define CUDACUHRE_QUAD_GPUQUAD_VOLUME_CUH
+namespace quad {
+// The integration box.
 template <typename T, int NDIM>
 struct Volume {
   T lows[NDIM] = {0.0};
   T highs[NDIM];
 
-  Volume() {
+  __host__ Volume() {
     for (T& x : highs) x = 1.0;
   }
-  Volume(std::array<T, NDIM> l, std::array<T, NDIM> h) {
+  __host__ Volume(std::array<T, NDIM> l, std::array<T, NDIM> h) {
     std::memcpy(lows, l.data(), NDIM * sizeof(T));
     std::memcpy(highs, h.data(), NDIM * sizeof(T));
   }
-  Volume(T const* l, T const* h) {
-    std::memcpy(lows, l, NDIM * sizeof(T));
-    std::memcpy(highs, h, NDIM * sizeof(T));
+  __host__ __device__ Volume(T const* l, T const* h) {
+    for (int i = 0; i < NDIM; ++i) {
+      lows[i] = l[i];
+      highs[i] = h[i];
+    }
   }
-  Volume(T l, T h) {
+  __host__ Volume(T l, T h) {
     for (int i = 0; i < NDIM; ++i) {
       lows[i] = l;
       highs[i] = h;
     }
   }
 };
+}  // namespace quad
+#endif
+
+namespace pagani {
+
+using integration_result = numint::integration_result;
+template <typename T, int NDIM>
+using Volume = quad::Volume<T, NDIM>;
 
 namespace detail {
 
@@ -324,13 +346,6 @@ integration_result mcubes_integrate(IntegT const& integrand, double epsrel, doub
 }  // namespace pagani
 
 #ifndef PAGANI_GB300_NO_REFERENCE_NAMES
-namespace quad {
-template <typename T, int NDIM>
-using Volume = pagani::Volume<T, NDIM>;
-}
-namespace numint {
-using integration_result = pagani::integration_result;
-}
 template <typename T, size_t ndim, int debug = 0, bool use_custom = false, bool collect_mult_runs = false>
 using Workspace = pagani::Workspace<T, ndim, debug, use_custom, collect_mult_runs>;
 

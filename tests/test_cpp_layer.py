@@ -35,6 +35,17 @@ def test_header_compiles():
     assert os.path.getsize(out) > 0
 
 
+@pytest.mark.parametrize("reference_first", [0, 1])
+def test_header_with_reference_types_either_order(reference_first):
+    """numint::integration_result and quad::Volume come from whichever header is
+    included first (the reference's integrand-side headers include them)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "interop_check.cu")
+    out = os.path.join(BUILD, f"interop_{reference_first}.o")
+    subprocess.check_call([_nvcc()] + _flags() + [f"-DREFERENCE_FIRST={reference_first}", "-c", src, "-o", out])
+    assert os.path.getsize(out) > 0
+
+
 @pytest.mark.gpu
 def test_workspace_functors_match_families(lib):
     from gpuintegration_gb300 import _build

@@ -33,14 +33,16 @@ def test_batch_equals_individual_runs(ctx):
                (b.estimate, b.errorest, b.nregions, b.status, b.iters, b.neval)
 
 
-def test_small_pool_admission_and_spill_keep_results(ctx):
+@pytest.mark.parametrize("count,pool,seed", [(12, 6000, 7), (40, 2500, 8)])
+def test_small_pool_admission_and_spill_keep_results(ctx, count, pool, seed):
     """With a pool far too small for the batch, integrals wait for admission and
-    over-capacity region lists move to host memory between iterations; every
-    result must still equal the integral's stand-alone result bit for bit."""
-    rng = np.random.default_rng(7)
-    fs = _mixed(rng, 12)
+    over-capacity region lists move to host memory (pinned spill slices, reused
+    across iterations) between iterations; every result must still equal the
+    integral's stand-alone result bit for bit."""
+    rng = np.random.default_rng(seed)
+    fs = _mixed(rng, count)
     eps = 10 ** rng.uniform(-5, -3.5, size=len(fs))
-    opt = pg.default_options(max_regions=6000)
+    opt = pg.default_options(max_regions=pool)
     batch = ctx.batch_integrate(fs, eps, 0.0, options=opt)
     for f, e, b in zip(fs, eps, batch):
         r = ctx.integrate(f, float(e), 0.0)

@@ -84,3 +84,12 @@ def test_split_axis_point_order(orc, d):
             assert t["set_of"][base + 2 * k] == s
             assert p[k] > 0 and m[k] < 0 and p[k] == -m[k]
             assert np.count_nonzero(p) == 1 and np.count_nonzero(m) == 1
+
+
+@pytest.mark.parametrize("d", list(range(2, 13)))
+def test_null_rule_norms_non_negative(lib, d):
+    """The evaluation kernel takes the null-rule maxima on the bit patterns of
+    |.| * norm, which orders them numerically only when every norm is >= 0."""
+    import gpuintegration_gb300 as pg
+    t = pg.rule_tables(d)
+    assert np.all(t["norm"] >= 0.0) and not np.any(np.signbit(t["norm"]))
