@@ -61,7 +61,7 @@ class PgResult(ctypes.Structure):
 class PgOptions(ctypes.Structure):
     _fields_ = [("relerr_classification", ctypes.c_int32), ("max_iters", ctypes.c_int32),
                 ("device_mem_model", ctypes.c_double), ("max_regions", ctypes.c_uint64),
-                ("eval_mode", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("eval_mode", ctypes.c_int32), ("predict_split", ctypes.c_int32)]
 
 
 class PgStats(ctypes.Structure):
@@ -70,7 +70,7 @@ class PgStats(ctypes.Structure):
                 ("eval_ms", ctypes.c_double), ("stage_ms", ctypes.c_double), ("stage_bytes", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("tune_warps", ctypes.c_int32 * 2), ("tune_ctas_per_sm", ctypes.c_int32 * 2),
-                ("eval_bytes", ctypes.c_uint64)]
+                ("eval_bytes", ctypes.c_uint64), ("host_ms", ctypes.c_double), ("sync_ms", ctypes.c_double)]
 
 
 class PgMcubesOptions(ctypes.Structure):
@@ -109,6 +109,9 @@ def load_library(path: str = LIB_PATH):
         "pg_context_reset_stats": (ctypes.c_int, [c_ctx]),
         "pg_context_stream": (ctypes.c_void_p, [c_ctx]),
         "pg_synchronize": (ctypes.c_int, [c_ctx]),
+        "pg_integrate_regions": (ctypes.c_int, [c_ctx, P(PgIntegrand), _D, _D, ctypes.c_uint64, ctypes.c_double,
+                                                ctypes.c_double, _D, _D, P(PgOptions), P(PgResult)]),
+        "pg_last_snapshot": (ctypes.c_int, [c_ctx, P(ctypes.c_int32), P(ctypes.c_uint64), _D, _D, ctypes.c_uint64]),
         "pg_integrate": (ctypes.c_int, [c_ctx, P(PgIntegrand), ctypes.c_double, ctypes.c_double, _D, _D,
                                         P(PgOptions), P(PgResult)]),
         "pg_evaluate_regions": (ctypes.c_int, [c_ctx, P(PgIntegrand), _D, _D, ctypes.c_uint64, _D, _D, _D, _D,
@@ -284,6 +287,42 @@ class Context:
         self._check(self.lib.pg_integrate(self.h, ctypes.byref(f.to_c()), epsrel, epsabs, _ptr(lo), _ptr(hi),
                                           ctypes.byref(o), ctypes.byref(r)))
         return IntegrationResult.from_c(r)
+
+    def integrate_regions(self, f: Integrand, left, length, epsrel: float, epsabs: float,
+                          vol: Optional[Volume] = None, relerr_classification: bool = True,
+                          predict_split: bool = False, options: Optional[PgOptions] = None) -> IntegrationResult:
+        """Workspace::integrate(f, subregions, ...) (Workspace.cuh:148-158): PAGANI from
+        the given first region list, SoA arrays of shape (ndim, n) in unit coordinates."""
+        o = options if options is not None else default_options()
+        o.relerr_classification = 1 if relerr_classification else 0
+        o.predict_split = 1 if predict_split else 0
+        left = np.ascontiguousarray(left, dtype=np.float64)
+        length = np.ascontiguousarray(length, dtype=np.float64)
+        if left.shape != length.shape or left.ndim != 2 or left.shape[0] != f.ndim:
+            raise ValueError("left and length must have shape (ndim, n)")
+        lo = hi = None
+        if vol is not None:
+            lo = np.ascontiguousarray(vol.lows, dtype=np.float64)
+            hi = np.ascontiguousarray(vol.highs, dtype=np.float64)
+        r = PgResult()
+        self._check(self.lib.pg_integrate_regions(self.h, ctypes.byref(f.to_c()), _ptr(left), _ptr(length),
+                                                  left.shape[1], epsrel, epsabs, _ptr(lo), _ptr(hi),
+                                                  ctypes.byref(o), ctypes.byref(r)))
+        return IntegrationResult.from_c(r)
+
+    def last_snapshot(self):
+        """The region list kept at iteration 15 by the last predict_split run
+        (Sub_regions::take_snapshot), as (left, length) of shape (ndim, n), or None."""
+        d = ctypes.c_int32()
+        n = ctypes.c_uint64()
+        self._check(self.lib.pg_last_snapshot(self.h, ctypes.byref(d), ctypes.byref(n), None, None, 0))
+        if n.value == 0:
+            return None
+        left = np.zeros((d.value, n.value))
+        length = np.zeros((d.value, n.value))
+        self._check(self.lib.pg_last_snapshot(self.h, ctypes.byref(d), ctypes.byref(n), _ptr(left), _ptr(length),
+                                              n.value))
+        return left, length
 
     def batch_integrate(self, fs: Sequence[Integrand], epsrel, epsabs, options: Optional[PgOptions] = None,
                         completion_ms: Optional[np.ndarray] = None):

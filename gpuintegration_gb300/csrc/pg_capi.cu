@@ -20,6 +20,10 @@ struct pg_context {
   pg::DevBuf s_left, s_len, s_est, s_err, s_err2, s_bis, s_act, s_par, s_out_left, s_out_len, s_owner, s_seg,
       s_chunks, s_trans, s_off, s_part, s_desc, s_x, s_res;
   pg::McubesState* mc = nullptr;
+  // region list kept by the last predict_split run
+  std::vector<double> snap_left, snap_length;
+  uint64_t snap_n = 0;
+  int32_t snap_d = 0;
 };
 
 namespace {
@@ -126,6 +130,7 @@ void pg_options_default(pg_options* opt) {
   opt->device_mem_model = 16e9;
   opt->max_regions = 0;
   opt->eval_mode = 0;
+  opt->predict_split = 0;
 }
 
 int pg_feval(int ndim) {
@@ -212,25 +217,71 @@ static int validate_eps(pg_context* ctx, double epsrel, double epsabs) {
   return PG_OK;
 }
 
-int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double epsabs, const double* lows,
-                 const double* highs, const pg_options* opt, pg_result* out) {
-  if (!ctx || !f || !out) return set_err(ctx, PG_BAD_ARG, "null argument");
-  int rc = validate_eps(ctx, epsrel, epsabs);
-  if (rc != PG_OK) return rc;
-  Guard g(ctx);
+// One integral through the engine: descriptor prepared by the caller,
+// optional first region list, predict_split snapshot kept in the context.
+static int run_single(pg_context* ctx, const pg::IntegralDesc& D, double epsrel, double epsabs, const pg_options* opt,
+                      const double* left, const double* length, uint64_t n, const pg::EvalLauncher& launch,
+                      pg_result* out) {
   std::vector<pg::Job> jobs(1);
-  std::string why;
-  rc = pg::prepare_desc(*f, lows, highs, &jobs[0].desc, &why);
-  if (rc != PG_OK) return set_err(ctx, rc, why);
+  jobs[0].desc = D;
   jobs[0].epsrel = epsrel;
   jobs[0].epsabs = epsabs;
   if (opt) jobs[0].opt = *opt; else pg_options_default(&jobs[0].opt);
   if (jobs[0].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
   if (jobs[0].opt.max_iters <= 0) jobs[0].opt.max_iters = 700;
-  rc = ctx->eng->run(jobs, pg::launch_family_eval);
+  if (n) {
+    if (!left || !length) return set_err(ctx, PG_BAD_ARG, "null region list");
+    for (uint64_t q = 0; q < n * (uint64_t)D.d; ++q)
+      if (!(length[q] > 0.0) || !std::isfinite(left[q]) || !std::isfinite(length[q]))
+        return set_err(ctx, PG_BAD_ARG, "region lists need finite coordinates and positive lengths");
+    jobs[0].init_left = left;
+    jobs[0].init_length = length;
+    jobs[0].init_n = n;
+  }
+  if (jobs[0].opt.predict_split) {
+    ctx->snap_n = 0;
+    ctx->snap_d = D.d;
+    jobs[0].snap_left = &ctx->snap_left;
+    jobs[0].snap_length = &ctx->snap_length;
+    jobs[0].snap_n = &ctx->snap_n;
+  }
+  int rc = ctx->eng->run(jobs, launch);
   if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
   *out = jobs[0].res;
   return out->status == 0 ? PG_OK : PG_NOT_CONVERGED;
+}
+
+int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double epsabs, const double* lows,
+                 const double* highs, const pg_options* opt, pg_result* out) {
+  return pg_integrate_regions(ctx, f, nullptr, nullptr, 0, epsrel, epsabs, lows, highs, opt, out);
+}
+
+int pg_integrate_regions(pg_context* ctx, const pg_integrand* f, const double* left, const double* length,
+                         uint64_t n, double epsrel, double epsabs, const double* lows, const double* highs,
+                         const pg_options* opt, pg_result* out) {
+  if (!ctx || !f || !out) return set_err(ctx, PG_BAD_ARG, "null argument");
+  int rc = validate_eps(ctx, epsrel, epsabs);
+  if (rc != PG_OK) return rc;
+  Guard g(ctx);
+  pg::IntegralDesc D;
+  std::string why;
+  rc = pg::prepare_desc(*f, lows, highs, &D, &why);
+  if (rc != PG_OK) return set_err(ctx, rc, why);
+  return run_single(ctx, D, epsrel, epsabs, opt, left, length, n, pg::launch_family_eval, out);
+}
+
+int pg_last_snapshot(pg_context* ctx, int32_t* ndim, uint64_t* n, double* left, double* length, uint64_t capacity) {
+  if (!ctx || !n) return set_err(ctx, PG_BAD_ARG, "null argument");
+  Guard g(ctx);
+  *n = ctx->snap_n;
+  if (ndim) *ndim = ctx->snap_d;
+  if (ctx->snap_n && left && length) {
+    if (capacity < ctx->snap_n) return set_err(ctx, PG_BAD_ARG, "snapshot buffers too small");
+    const size_t m = ctx->snap_n * (size_t)ctx->snap_d;
+    std::memcpy(left, ctx->snap_left.data(), m * 8);
+    std::memcpy(length, ctx->snap_length.data(), m * 8);
+  }
+  return PG_OK;
 }
 
 int pg_batch_integrate(pg_context* ctx, uint64_t count, const pg_integrand* fs, const double* epsrel,
@@ -373,23 +424,23 @@ static pg::EvalLauncher user_launcher(pg_eval_launcher fn, void* user) {
 int pg_integrate_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user, double epsrel,
                           double epsabs, const double* lows, const double* highs, const pg_options* opt,
                           pg_result* out) {
+  return pg_integrate_regions_launcher(ctx, ndim, launch, user, nullptr, nullptr, 0, epsrel, epsabs, lows, highs,
+                                       opt, out);
+}
+
+int pg_integrate_regions_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user,
+                                  const double* left, const double* length, uint64_t n, double epsrel,
+                                  double epsabs, const double* lows, const double* highs, const pg_options* opt,
+                                  pg_result* out) {
   if (!ctx || !launch || !out) return set_err(ctx, PG_BAD_ARG, "null argument");
   int rc = validate_eps(ctx, epsrel, epsabs);
   if (rc != PG_OK) return rc;
   Guard g(ctx);
-  std::vector<pg::Job> jobs(1);
+  pg::IntegralDesc D;
   std::string why;
-  rc = pg::prepare_user_desc(ndim, lows, highs, &jobs[0].desc, &why);
+  rc = pg::prepare_user_desc(ndim, lows, highs, &D, &why);
   if (rc != PG_OK) return set_err(ctx, rc, why);
-  jobs[0].epsrel = epsrel;
-  jobs[0].epsabs = epsabs;
-  if (opt) jobs[0].opt = *opt; else pg_options_default(&jobs[0].opt);
-  if (jobs[0].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
-  if (jobs[0].opt.max_iters <= 0) jobs[0].opt.max_iters = 700;
-  rc = ctx->eng->run(jobs, user_launcher(launch, user));
-  if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
-  *out = jobs[0].res;
-  return out->status == 0 ? PG_OK : PG_NOT_CONVERGED;
+  return run_single(ctx, D, epsrel, epsabs, opt, left, length, n, user_launcher(launch, user), out);
 }
 
 int pg_evaluate_regions_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user,

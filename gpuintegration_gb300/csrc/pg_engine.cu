@@ -602,7 +602,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     J.cls.required_digits = (int)std::ceil(std::log10(1 / J.epsrel));
     J.cls.ndim = J.desc.d;
     J.cls.total_mem = J.opt.device_mem_model > 0 ? J.opt.device_mem_model : 16e9;
-    J.n = ipow_u((uint64_t)parts_for(J.desc.d), J.desc.d);
+    J.n = J.init_n ? J.init_n : ipow_u((uint64_t)parts_for(J.desc.d), J.desc.d);
     J.start = J.par_start = 0;
     J.has_parent = 0;
     J.iters = 0;
@@ -613,6 +613,10 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   }
   spill_.reset();
   const auto t_start = std::chrono::steady_clock::now();
+  // Host decision time: from the end of an iteration's readback to the next
+  // evaluation launch (the device idles in between unless work is queued).
+  bool decision_open = false;
+  auto t_decision = t_start;
   int cur = 0;
   uint64_t T = 0, P = 0;  // regions and parent estimates in the current list
   uint32_t first_waiting = 0;
@@ -641,7 +645,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       uint64_t t = T, pp = P;
       uint64_t* hs = (uint64_t*)h_adm_starts_.p;
       uint32_t* hi = (uint32_t*)h_adm_ids_.p;
-      std::vector<uint32_t> restore;
+      std::vector<uint32_t> restore, custom;
       while (first_waiting < njobs && jobs[first_waiting].state == JOB_DONE) ++first_waiting;
       for (uint32_t j = first_waiting; j < njobs; ++j) {
         Job& J = jobs[j];
@@ -654,6 +658,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
         if (J.state == JOB_SPILLED) {
           pp += J.n / 2;
           restore.push_back(j);
+        } else if (J.init_n) {
+          custom.push_back(j);
         } else {
           hs[adm_pending.size()] = J.start;
           hi[adm_pending.size()] = j;
@@ -674,6 +680,19 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
               (const uint64_t*)adm_starts_.p, (const uint32_t*)adm_ids_.p, (const IntegralDesc*)descs_.p, m);
           stats.launches++;
           PG_TRY(cudaGetLastError(), "uniform split launch");
+        }
+        for (uint32_t j : custom) {  // caller-given first lists (pageable host memory: synchronous copies)
+          Job& J = jobs[j];
+          const int d = J.desc.d;
+          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, J.init_left, J.n * 8, J.n * 8,
+                                   d, cudaMemcpyHostToDevice, stream_), "initial regions");
+          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, J.init_length, J.n * 8,
+                                   J.n * 8, d, cudaMemcpyHostToDevice, stream_), "initial regions");
+          fill_owner_kernel<<<(unsigned)div_up(J.n, 256), 256, 0, stream_>>>((uint32_t*)owner_[cur].p, J.start, J.n,
+                                                                            j);
+          stats.launches++;
+          PG_TRY(cudaGetLastError(), "initial regions launch");
+          stats.h2d_bytes += J.n * 16 * d;
         }
         for (uint32_t j : restore) {
           Job& J = jobs[j];
@@ -735,7 +754,10 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       S.chunk_start = (uint32_t)chunk_list.size();
       S.nchunks = (uint32_t)div_up(S.n, kChunk);
       S.has_parent = J.has_parent;
-      S.relerr = J.opt.relerr_classification;
+      // predict_split (Workspace.cuh:415-420): no rel-err classification while
+      // the list is small, in the first 15 iterations, and nothing finished yet.
+      S.relerr = J.opt.predict_split ? !(J.n <= 15000000ull && J.iters < 15 && J.res.nregions == 0)
+                                     : J.opt.relerr_classification;
       S.epsrel = J.epsrel;
       for (uint32_t b = 0; b < S.nchunks; ++b) chunk_list.push_back(ChunkRef{j, b});
       hs[j] = S;
@@ -764,6 +786,10 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     EvalLaunch L{(const double*)left_[cur].p, (const double*)len_[cur].p, N, reg_cap_[cur],
                  (const uint32_t*)owner_[cur].p, (const IntegralDesc*)descs_.p, &rule_, (double*)est_.p,
                  (double*)err_a_.p, (int32_t*)bisect_.p, maxd, num_sms, stream_, tn.warps, tn.ctas_per_sm};
+    if (decision_open) {
+      stats.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_decision).count();
+      decision_open = false;
+    }
     if (profiling) cudaEventRecord(ev_[0], stream_);
     PG_TRY(launch(L), "evaluation launch");
     stats.launches++;
@@ -786,7 +812,13 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     if (profiling) cudaEventRecord(ev_[2], stream_);
     PG_TRY(cudaMemcpyAsync(h_scal_.p, scal_.p, njobs * sizeof(IterScalars), cudaMemcpyDeviceToHost, stream_),
            "scalar readback");
-    PG_TRY(cudaStreamSynchronize(stream_), "iteration");
+    {
+      const auto w0 = std::chrono::steady_clock::now();
+      PG_TRY(cudaStreamSynchronize(stream_), "iteration");
+      t_decision = std::chrono::steady_clock::now();
+      decision_open = true;
+      stats.sync_ms += std::chrono::duration<double, std::milli>(t_decision - w0).count();
+    }
     stats.d2h_bytes += njobs * sizeof(IterScalars);
     stats.stage_bytes += N * 29;
     if (profiling) {
@@ -807,6 +839,19 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       keepA[j] = 0;
       const double iter_est = S.iter_est, iter_err = S.iter_err;
       const double cest = std::fabs(cum.estimate + iter_est), cerr = cum.errorest + iter_err;
+      if (J.opt.predict_split && J.snap_n && J.iters == 15 && cum.nregions == 0) {
+        // take_snapshot of the list evaluated in iteration 15 (Workspace.cuh:437-441)
+        const int d = J.desc.d;
+        J.snap_left->resize(n * d);
+        J.snap_length->resize(n * d);
+        PG_TRY(cudaMemcpy2DAsync(J.snap_left->data(), n * 8, (const double*)left_[cur].p + J.start, reg_cap_[cur] * 8,
+                                 n * 8, d, cudaMemcpyDeviceToHost, stream_), "snapshot");
+        PG_TRY(cudaMemcpy2DAsync(J.snap_length->data(), n * 8, (const double*)len_[cur].p + J.start,
+                                 reg_cap_[cur] * 8, n * 8, d, cudaMemcpyDeviceToHost, stream_), "snapshot");
+        PG_TRY(cudaStreamSynchronize(stream_), "snapshot");
+        *J.snap_n = n;
+        stats.d2h_bytes += n * 16 * d;
+      }
       J.iters++;
       if (cerr / cest <= J.epsrel || cerr <= J.epsabs) {  // accuracy_reached (PaganiUtils.cuh:387-394)
         cum.estimate += iter_est;

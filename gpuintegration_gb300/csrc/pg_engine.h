@@ -117,6 +117,16 @@ struct Job {
   // parent estimates.
   double* sp = nullptr;
   size_t sp_bytes = 0;
+  // Caller-given initial region list (host, SoA [dim * init_n + i]); 0
+  // regions: the uniform split (Workspace.cuh:379-387).
+  const double* init_left = nullptr;
+  const double* init_length = nullptr;
+  uint64_t init_n = 0;
+  // With opt.predict_split: receives the region list of iteration 15
+  // (Workspace.cuh:437-441), SoA [dim * n + i].
+  std::vector<double>* snap_left = nullptr;
+  std::vector<double>* snap_length = nullptr;
+  uint64_t* snap_n = nullptr;
 };
 
 // Pinned host storage for region lists moved out of the device pool.  Blocks

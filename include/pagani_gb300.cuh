@@ -44,6 +44,7 @@
 #include <string>
 #include <type_traits>
 #include <utility>
+#include <vector>
 
 #include "pagani_gb300.h"
 #include "../gpuintegration_gb300/csrc/pg_eval.cuh"
@@ -234,6 +235,134 @@ inline integration_result to_result(const pg_result& r) {
 
 }  // namespace detail
 
+// Sub_regions (cuda/pagani/quad/GPUquad/Sub_regions.cuh:38-258): a region
+// list in unit coordinates, SoA [dim * size + i], on the device (dLeftCoord,
+// dLength) with a host mirror (LeftCoord, Length), and the snapshot that a
+// predict_split run keeps at iteration 15.
+template <typename T, size_t ndim>
+struct Sub_regions {
+  static_assert(std::is_same<T, double>::value, "region lists are double precision");
+
+  Sub_regions() {}
+  explicit Sub_regions(const size_t partitions_per_axis) { uniform_split(partitions_per_axis); }
+  Sub_regions(const Sub_regions& other) {
+    device_init(other.size);
+    cudaMemcpy(dLeftCoord, other.dLeftCoord, sizeof(T) * size * ndim, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(dLength, other.dLength, sizeof(T) * size * ndim, cudaMemcpyDeviceToDevice);
+  }
+  Sub_regions& operator=(const Sub_regions&) = delete;
+  ~Sub_regions() {
+    delete[] LeftCoord;
+    delete[] Length;
+    cudaFree(dLeftCoord);
+    cudaFree(dLength);
+    cudaFree(snapshot_dLeftCoord);
+    cudaFree(snapshot_dLength);
+  }
+
+  void host_init() {
+    delete[] LeftCoord;
+    delete[] Length;
+    host_data_size = size;
+    LeftCoord = new T[size * ndim];
+    Length = new T[size * ndim];
+  }
+  void device_init(const size_t numRegions) {
+    cudaFree(dLeftCoord);
+    cudaFree(dLength);
+    size = numRegions;
+    dLeftCoord = nullptr;
+    dLength = nullptr;
+    cudaMalloc((void**)&dLeftCoord, sizeof(T) * numRegions * ndim);
+    cudaMalloc((void**)&dLength, sizeof(T) * numRegions * ndim);
+  }
+  void host_device_init(const size_t numRegions) {
+    device_init(numRegions);
+    host_init();
+  }
+  void refresh_host_device() {
+    if (host_data_size != size || !LeftCoord) host_init();
+    cudaMemcpy(LeftCoord, dLeftCoord, sizeof(T) * size * ndim, cudaMemcpyDeviceToHost);
+    cudaMemcpy(Length, dLength, sizeof(T) * size * ndim, cudaMemcpyDeviceToHost);
+  }
+  void refresh_device_from_host() {
+    cudaMemcpy(dLeftCoord, LeftCoord, sizeof(T) * size * ndim, cudaMemcpyHostToDevice);
+    cudaMemcpy(dLength, Length, sizeof(T) * size * ndim, cudaMemcpyHostToDevice);
+  }
+
+  // p^ndim equal cells: cell i has index (i / p^k) % p on axis k
+  // (Sub_regions.cuh:164-185).
+  void uniform_split(const size_t p) {
+    size_t count = 1;
+    for (size_t k = 0; k < ndim; ++k) count *= p;
+    const T len = 1.0 / (T)p;
+    device_init(count);
+    host_init();
+    for (size_t i = 0; i < count; ++i) {
+      size_t q = i;
+      for (size_t k = 0; k < ndim; ++k) {
+        const size_t id = q % p;
+        q /= p;
+        LeftCoord[k * count + i] = (T)id * len;
+        Length[k * count + i] = len;
+      }
+    }
+    refresh_device_from_host();
+  }
+
+  T compute_region_volume(const size_t regionID) {
+    T reg_vol = 1.;
+    for (size_t dim = 0; dim < ndim; dim++) reg_vol *= Length[size * dim + regionID];
+    return reg_vol;
+  }
+  T compute_total_volume() {
+    refresh_host_device();
+    T total_vol = 0.;
+    for (size_t i = 0; i < size; i++) total_vol += compute_region_volume(i);
+    return total_vol;
+  }
+  quad::Volume<T, (int)ndim> extract_region(const size_t regionID) {
+    refresh_host_device();
+    quad::Volume<T, (int)ndim> b;
+    for (size_t dim = 0; dim < ndim; dim++) {
+      b.lows[dim] = LeftCoord[size * dim + regionID];
+      b.highs[dim] = LeftCoord[size * dim + regionID] + Length[size * dim + regionID];
+    }
+    return b;
+  }
+
+  void take_snapshot() {
+    cudaFree(snapshot_dLeftCoord);
+    cudaFree(snapshot_dLength);
+    snapshot_size = size;
+    cudaMalloc((void**)&snapshot_dLeftCoord, sizeof(T) * size * ndim);
+    cudaMalloc((void**)&snapshot_dLength, sizeof(T) * size * ndim);
+    cudaMemcpy(snapshot_dLeftCoord, dLeftCoord, sizeof(T) * size * ndim, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(snapshot_dLength, dLength, sizeof(T) * size * ndim, cudaMemcpyDeviceToDevice);
+  }
+  // The snapshot becomes the region list (Sub_regions.cuh:231-239).
+  void load_snapshot() {
+    cudaFree(dLeftCoord);
+    cudaFree(dLength);
+    dLeftCoord = snapshot_dLeftCoord;
+    dLength = snapshot_dLength;
+    size = snapshot_size;
+    snapshot_dLeftCoord = nullptr;
+    snapshot_dLength = nullptr;
+    snapshot_size = 0;
+  }
+
+  T* LeftCoord = nullptr;
+  T* Length = nullptr;
+  T* dLeftCoord = nullptr;
+  T* dLength = nullptr;
+  T* snapshot_dLeftCoord = nullptr;
+  T* snapshot_dLength = nullptr;
+  size_t size = 0;
+  size_t host_data_size = 0;
+  size_t snapshot_size = 0;
+};
+
 // Workspace (cuda/pagani/quad/GPUquad/Workspace.cuh:23-70): one PAGANI
 // integrator on the current CUDA device.  It owns a library context (region
 // pool, stream, rule tables), created at the first integrate call and kept for
@@ -254,21 +383,26 @@ class Workspace {
   Workspace(const Workspace&) = delete;
   Workspace& operator=(const Workspace&) = delete;
 
+  // From the uniform split (Workspace.cuh:361-368).  predict_split: no
+  // rel-err classification in the first 15 iterations while the list is small
+  // and nothing has finished (Workspace.cuh:415-420).  collect_iters (debug
+  // output of the reference) is accepted and ignored.
   template <typename IntegT, bool predict_split = false, bool collect_iters = false>
   integration_result integrate(const IntegT& integrand, T epsrel, T epsabs, Volume<T, (int)ndim> const& vol,
                                bool relerr_classification = true) {
-    static_assert(!predict_split, "predict_split (region snapshot and reload) is not part of this library");
-    using Fn = detail::UserFn<IntegT, ndim>;
-    detail::FunctorCopy<IntegT, ndim> copy(integrand);
-    pg_options opt;
-    pg_options_default(&opt);
-    opt.relerr_classification = relerr_classification ? 1 : 0;
-    pg_result r;
-    std::memset(&r, 0, sizeof r);
-    const int rc = pg_integrate_launcher(context(), (int32_t)ndim, &detail::launch_user<Fn, ndim>,
-                                         (void*)&copy.fn, epsrel, epsabs, vol.lows, vol.highs, &opt, &r);
-    if (rc < 0) throw std::runtime_error(std::string("pagani::Workspace::integrate: ") + pg_last_error(ctx_));
-    return detail::to_result(r);
+    return run<IntegT, predict_split>(integrand, nullptr, epsrel, epsabs, vol, relerr_classification);
+  }
+
+  // From the caller's region list (Workspace.cuh:148-158); with predict_split
+  // the list of iteration 15 is kept in subregions' snapshot
+  // (Workspace.cuh:437-441).  `optional` names the run in the reference's
+  // debug output and is ignored.
+  template <typename IntegT, bool predict_split = false, bool collect_iters = false>
+  integration_result integrate(const IntegT& integrand, Sub_regions<T, ndim>& subregions, T epsrel, T epsabs,
+                               Volume<T, (int)ndim> const& vol, bool relerr_classification = true,
+                               const std::string& optional = "default") {
+    (void)optional;
+    return run<IntegT, predict_split>(integrand, &subregions, epsrel, epsabs, vol, relerr_classification);
   }
 
   // Region evaluation of the functor on caller-given regions (SoA
@@ -287,6 +421,51 @@ class Workspace {
       throw std::runtime_error(std::string("pagani::Workspace::evaluate_regions: ") + pg_last_error(ctx_));
   }
 
+ private:
+  template <typename IntegT, bool predict_split>
+  integration_result run(const IntegT& integrand, Sub_regions<T, ndim>* sub, T epsrel, T epsabs,
+                         Volume<T, (int)ndim> const& vol, bool relerr_classification) {
+    using Fn = detail::UserFn<IntegT, ndim>;
+    detail::FunctorCopy<IntegT, ndim> copy(integrand);
+    pg_options opt;
+    pg_options_default(&opt);
+    opt.relerr_classification = relerr_classification ? 1 : 0;
+    opt.predict_split = predict_split ? 1 : 0;
+    pg_result r;
+    std::memset(&r, 0, sizeof r);
+    const T* left = nullptr;
+    const T* length = nullptr;
+    uint64_t n = 0;
+    if (sub) {
+      sub->refresh_host_device();
+      left = sub->LeftCoord;
+      length = sub->Length;
+      n = sub->size;
+    }
+    const int rc = pg_integrate_regions_launcher(context(), (int32_t)ndim, &detail::launch_user<Fn, ndim>,
+                                                 (void*)&copy.fn, left, length, n, epsrel, epsabs, vol.lows,
+                                                 vol.highs, &opt, &r);
+    if (rc < 0) throw std::runtime_error(std::string("pagani::Workspace::integrate: ") + pg_last_error(ctx_));
+    if (sub && predict_split) {
+      int32_t d = 0;
+      uint64_t sn = 0;
+      pg_last_snapshot(ctx_, &d, &sn, nullptr, nullptr, 0);
+      if (sn) {
+        std::vector<T> sl(sn * ndim), sd(sn * ndim);
+        pg_last_snapshot(ctx_, &d, &sn, sl.data(), sd.data(), sn);
+        cudaFree(sub->snapshot_dLeftCoord);
+        cudaFree(sub->snapshot_dLength);
+        cudaMalloc((void**)&sub->snapshot_dLeftCoord, sizeof(T) * sn * ndim);
+        cudaMalloc((void**)&sub->snapshot_dLength, sizeof(T) * sn * ndim);
+        cudaMemcpy(sub->snapshot_dLeftCoord, sl.data(), sizeof(T) * sn * ndim, cudaMemcpyHostToDevice);
+        cudaMemcpy(sub->snapshot_dLength, sd.data(), sizeof(T) * sn * ndim, cudaMemcpyHostToDevice);
+        sub->snapshot_size = (size_t)sn;
+      }
+    }
+    return detail::to_result(r);
+  }
+
+ public:
   // The library context (created on the current device at first use).
   pg_context* context() {
     if (!ctx_) {
@@ -348,6 +527,8 @@ integration_result mcubes_integrate(IntegT const& integrand, double epsrel, doub
 #ifndef PAGANI_GB300_NO_REFERENCE_NAMES
 template <typename T, size_t ndim, int debug = 0, bool use_custom = false, bool collect_mult_runs = false>
 using Workspace = pagani::Workspace<T, ndim, debug, use_custom, collect_mult_runs>;
+template <typename T, size_t ndim>
+using Sub_regions = pagani::Sub_regions<T, ndim>;
 
 namespace cuda_mcubes {
 // cuda/mcubes/vegasT.cuh:999-1030 (GeneratorType is accepted and ignored: the

@@ -102,7 +102,9 @@ typedef struct pg_options {
   double device_mem_model;  /* bytes seen by the memory-pressure classifier */
   uint64_t max_regions;     /* hard cap of the region pool (0 = derived from the model) */
   int32_t eval_mode;        /* must be 0: per-region rule sums in the reference's order */
-  int32_t reserved;
+  int32_t predict_split;    /* 1: the reference's predict_split variant (Workspace.cuh:415-441): no rel-err
+                               classification in the first 15 iterations while the list has <= 15e6 regions and
+                               nothing has finished; the list of iteration 15 is kept (pg_last_snapshot) */
 } pg_options;
 
 typedef struct pg_context pg_context;
@@ -121,6 +123,8 @@ typedef struct pg_stats {
   int32_t tune_warps[2];        /* autotuned regions per block: [0] ndim <= 8, [1] ndim > 8 */
   int32_t tune_ctas_per_sm[2];  /* autotuned grid cap (blocks per SM) of the evaluation kernel */
   uint64_t eval_bytes;          /* algorithmic HBM bytes of the evaluation launches */
+  double host_ms;               /* host time from an iteration's readback to the next evaluation launch */
+  double sync_ms;               /* host time blocked waiting for an iteration's device work */
 } pg_stats;
 
 void pg_options_default(pg_options* opt);
@@ -144,6 +148,22 @@ int pg_synchronize(pg_context* ctx);
  * for the unit cube. */
 int pg_integrate(pg_context* ctx, const pg_integrand* f, double epsrel, double epsabs, const double* lows,
                  const double* highs, const pg_options* opt, pg_result* out);
+
+/* PAGANI from a caller-given first region list: the reference's
+ * Workspace::integrate(f, subregions, epsrel, epsabs, vol, relerr, optional)
+ * overload (cuda/pagani/quad/GPUquad/Workspace.cuh:148-158).  n regions in the
+ * unit coordinates of [lows, highs], host SoA [dim * n + i] (the layout of
+ * Sub_regions, Sub_regions.cuh:38-258). */
+int pg_integrate_regions(pg_context* ctx, const pg_integrand* f, const double* left, const double* length,
+                         uint64_t n, double epsrel, double epsabs, const double* lows, const double* highs,
+                         const pg_options* opt, pg_result* out);
+
+/* The region list the last pg_integrate / pg_integrate_regions (or their
+ * launcher forms) with opt->predict_split kept at iteration 15
+ * (Sub_regions::take_snapshot, Sub_regions.cuh:220-229).  *n receives its
+ * region count (0: none kept) and *ndim its dimension; left/length (SoA
+ * [dim * n + i], may be NULL) receive it when capacity >= *n. */
+int pg_last_snapshot(pg_context* ctx, int32_t* ndim, uint64_t* n, double* left, double* length, uint64_t capacity);
 
 /* Region evaluation on a caller-given region list (host buffers, SoA
  * [dim * n + i]).  Replaces Cubature_rules::apply_cubature_integration_rules
@@ -193,6 +213,12 @@ typedef int (*pg_eval_launcher)(const pg_eval_args* args, void* user);
 int pg_integrate_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user, double epsrel,
                           double epsabs, const double* lows, const double* highs, const pg_options* opt,
                           pg_result* out);
+
+/* pg_integrate_regions for a user integrand. */
+int pg_integrate_regions_launcher(pg_context* ctx, int32_t ndim, pg_eval_launcher launch, void* user,
+                                  const double* left, const double* length, uint64_t n, double epsrel,
+                                  double epsabs, const double* lows, const double* highs, const pg_options* opt,
+                                  pg_result* out);
 
 /* pg_evaluate_regions for a user integrand (host buffers, SoA [dim * n + i]):
  * the region-evaluation stage test (test/cuda/pagani/RegionSampling.cu:48-88)

@@ -59,6 +59,11 @@ def load():
     lib.orc_integrate.restype = ctypes.c_int
     lib.orc_integrate.argtypes = [vp, ctypes.c_double, ctypes.c_double, _D, _D, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, ctypes.c_int, P(OrcResult), _D, ctypes.c_int]
+    lib.orc_integrate_regions.restype = ctypes.c_int
+    lib.orc_integrate_regions.argtypes = [vp, ctypes.c_double, ctypes.c_double, _D, _D, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _D, ctypes.c_uint64,
+                                          ctypes.c_int, _D, _D, ctypes.c_uint64, P(ctypes.c_uint64), P(OrcResult),
+                                          _D, ctypes.c_int]
     lib.orc_philox.argtypes = [P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_uint32)]
     if hasattr(lib, "orc_mcubes_integrate"):
         lib.orc_mcubes_integrate.restype = ctypes.c_int
@@ -168,6 +173,37 @@ def integrate(f, epsrel, epsabs, lows=None, highs=None, relerr_classification=Tr
                            device_mem, max_iters, nthreads or os.cpu_count() or 1, ctypes.byref(r), _p(tr), trace_cap)
     assert nt >= 0, nt
     return r, tr[:nt]
+
+
+def integrate_regions(f, left, length, epsrel, epsabs, lows=None, highs=None, relerr_classification=True,
+                      predict_split=False, device_mem=16e9, max_iters=700, nthreads=None, snap_cap=0):
+    """Workspace::integrate from a first region list (None: the uniform split),
+    with the predict_split variant; returns (result, snapshot or None)."""
+    lib = load()
+    d = f.ndim
+    lows = np.zeros(d) if lows is None else np.ascontiguousarray(lows, dtype=np.float64)
+    highs = np.ones(d) if highs is None else np.ascontiguousarray(highs, dtype=np.float64)
+    n = 0
+    if left is not None:
+        left = np.ascontiguousarray(left, dtype=np.float64)
+        length = np.ascontiguousarray(length, dtype=np.float64)
+        n = left.shape[1]
+    sl = np.zeros(d * max(snap_cap, 1))  # filled as SoA (d, n) over the first d * n entries
+    sn = np.zeros(d * max(snap_cap, 1))
+    snap_n = ctypes.c_uint64()
+    r = OrcResult()
+    s = _integrand_struct(f)
+    nt = lib.orc_integrate_regions(ctypes.byref(s), epsrel, epsabs, _p(lows), _p(highs),
+                                   1 if relerr_classification else 0, device_mem, max_iters,
+                                   nthreads or os.cpu_count() or 1, _p(left), _p(length), n,
+                                   1 if predict_split else 0, _p(sl), _p(sn), snap_cap, ctypes.byref(snap_n),
+                                   ctypes.byref(r), None, 0)
+    assert nt >= 0, nt
+    snap = None
+    if snap_n.value:
+        k = snap_n.value
+        snap = (k, (sl[:d * k].reshape(d, k).copy(), sn[:d * k].reshape(d, k).copy()) if snap_cap >= k else None)
+    return r, snap
 
 
 def philox(ctr, key):

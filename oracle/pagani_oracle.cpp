@@ -811,18 +811,36 @@ uint64_t orc_filter_split(int ndim, uint64_t n, const double* left, const double
 // (Workspace.cuh:361-494), with fix_error_budget_overflow (:121-146) and
 // heuristic_classify (:74-118).  trace (optional) receives, per iteration,
 // [N, A_after_classification, iter_est, iter_err, cumm_est, cumm_err].
-int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const double* lows, const double* highs,
-                  int relerr_classification, double total_device_mem, int max_iters, int nthreads, orc_result* out,
-                  double* trace, int trace_cap) {
+// Workspace::integrate (Workspace.cuh:148-358,361-494): from the uniform
+// split (init_n == 0) or from a caller-given first list (the Sub_regions
+// overload); with predict_split, rel-err classification is off while the list
+// has <= 15e6 regions, in the first 15 iterations and before anything finished
+// (Workspace.cuh:415-420), and the list of iteration 15 is copied out
+// (Workspace.cuh:437-441) when snap_cap allows.
+int orc_integrate_regions(const orc::Integrand* f, double epsrel, double epsabs, const double* lows,
+                          const double* highs, int relerr_classification, double total_device_mem, int max_iters,
+                          int nthreads, const double* init_left, const double* init_len, uint64_t init_n,
+                          int predict_split, double* snap_left, double* snap_len, uint64_t snap_cap,
+                          uint64_t* snap_n, orc_result* out, double* trace, int trace_cap) {
   using namespace orc;
   const int d = f->ndim;
   if (d < 2 || d > 15 || !out) return -1;
   const Rule R = make_rule(d);
   const Prepared P = prepare(*f);
   const int parts = d < 5 ? 4 : (d <= 10 ? 2 : 1);
-  size_t n = orc_uniform_split(d, parts, nullptr, nullptr);
-  std::vector<double> left(n * d), len(n * d);
-  orc_uniform_split(d, parts, left.data(), len.data());
+  size_t n;
+  std::vector<double> left, len;
+  if (init_n) {
+    n = init_n;
+    left.assign(init_left, init_left + n * d);
+    len.assign(init_len, init_len + n * d);
+  } else {
+    n = orc_uniform_split(d, parts, nullptr, nullptr);
+    left.resize(n * d);
+    len.resize(n * d);
+    orc_uniform_split(d, parts, left.data(), len.data());
+  }
+  if (snap_n) *snap_n = 0;
   std::vector<double> parent_est, parent_err;
   bool have_parent = false;
   Classifier C;
@@ -847,13 +865,21 @@ int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const d
     evaluate_all(R, P, lows, highs, n, left.data(), len.data(), est.data(), err.data(), bis.data(), nthreads);
     cum.neval += n * fev;
     const double iter_est = canon_sum(n, [&](size_t i) { return est[i]; });
+    const bool relerr =
+        predict_split ? !(n <= 15000000 && it < 15 && cum.nregions == 0) : relerr_classification != 0;
     if (have_parent) {
       nerr.assign(n, 0);
-      two_level(n, est.data(), err.data(), parent_est.data(), nerr.data(), act.data(), epsrel,
-                relerr_classification != 0);
+      two_level(n, est.data(), err.data(), parent_est.data(), nerr.data(), act.data(), epsrel, relerr);
       err.swap(nerr);
     }
     const double iter_err = canon_sum(n, [&](size_t i) { return err[i]; });
+    if (predict_split && cum.nregions == 0 && it == 15 && snap_n) {
+      *snap_n = n;
+      if (snap_left && snap_len && snap_cap >= n) {
+        std::copy(left.begin(), left.begin() + n * d, snap_left);
+        std::copy(len.begin(), len.begin() + n * d, snap_len);
+      }
+    }
     double* tr = (trace && ntrace < trace_cap) ? trace + 6 * ntrace : nullptr;
     if (tr) {
       tr[0] = (double)n;
@@ -949,6 +975,13 @@ int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const d
   cum.nregions += n;
   *out = cum;
   return ntrace;
+}
+
+int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const double* lows, const double* highs,
+                  int relerr_classification, double total_device_mem, int max_iters, int nthreads, orc_result* out,
+                  double* trace, int trace_cap) {
+  return orc_integrate_regions(f, epsrel, epsabs, lows, highs, relerr_classification, total_device_mem, max_iters,
+                               nthreads, nullptr, nullptr, 0, 0, nullptr, nullptr, 0, nullptr, out, trace, trace_cap);
 }
 
 }  // extern "C"

@@ -281,6 +281,48 @@ int main() {
     if (bad) ++failures;
   }
 
+  // Sub_regions overload (Workspace.cuh:148-158): a 5 x 5 first list, and
+  // predict_split with its iteration-15 snapshot (Workspace.cuh:415-441).
+  {
+    PeakProduct<2> p;
+    pg_integrand fam;
+    std::memset(&fam, 0, sizeof fam);
+    fam.family = PG_FAMILY_PRODUCT_PEAK;
+    fam.ndim = 2;
+    for (int k = 0; k < 2; ++k) {
+      fam.a[k] = 30.0;
+      fam.u[k] = k ? 0.61 : 0.37;
+      p.ia2[k] = 1.0 / (fam.a[k] * fam.a[k]);
+      p.u[k] = fam.u[k];
+    }
+    Workspace<double, 2> ws;
+    Sub_regions<double, 2> five(5);
+    const auto u = ws.integrate(p, five, 1e-6, 0.0, quad::Volume<double, 2>());
+    five.refresh_host_device();
+    pg_result f;
+    pg_integrate_regions(ctx, &fam, five.LeftCoord, five.Length, five.size, 1e-6, 0.0, nullptr, nullptr, nullptr, &f);
+    report("subregions5x5_peak2", u, f);
+
+    Sub_regions<double, 2> four(4);
+    const auto up = ws.integrate<PeakProduct<2>, true>(p, four, 1e-13, 0.0, quad::Volume<double, 2>());
+    pg_options opt;
+    pg_options_default(&opt);
+    opt.predict_split = 1;
+    pg_integrate(ctx, &fam, 1e-13, 0.0, nullptr, nullptr, &opt, &f);
+    report("predict_split_peak2", up, f);
+    int32_t sd = 0;
+    uint64_t sn = 0;
+    pg_last_snapshot(ctx, &sd, &sn, nullptr, nullptr, 0);
+    std::vector<double> sl(sn * 2), sL(sn * 2), dl(four.snapshot_size * 2), dL(four.snapshot_size * 2);
+    pg_last_snapshot(ctx, &sd, &sn, sl.data(), sL.data(), sn);
+    cudaMemcpy(dl.data(), four.snapshot_dLeftCoord, dl.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(dL.data(), four.snapshot_dLength, dL.size() * 8, cudaMemcpyDeviceToHost);
+    const bool ok = sn == (uint64_t)16 * 32768 && four.snapshot_size == sn && dl == sl && dL == sL;
+    std::printf("%s predict_split_snapshot %llu %zu\n", ok ? "PASS" : "FAIL", (unsigned long long)sn,
+                four.snapshot_size);
+    if (!ok) ++failures;
+  }
+
   // m-Cubes: functor vs family, same seed, same geometry (cuda/mcubes/vegasT.cuh:999-1030).
   {
     const double sigma = 0.1, c = 1.0 / (sigma * std::sqrt(2.0 * 3.14159265358979323846));

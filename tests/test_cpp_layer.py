@@ -61,5 +61,6 @@ def test_workspace_functors_match_families(lib):
     assert lines and lines[-1].startswith("DONE 0 failures")
     names = {ln.split()[1] for ln in lines if ln.startswith("PASS")}
     for case in ("gauss3_unit", "gauss5_box", "gauss8_unit", "gauss10_unit", "peak6_box_norelerr", "xy_unit",
-                 "xy_value", "nan3", "tabulated3", "regions5", "mcubes_gauss3", "quad_mcubes_gauss3", "mcubes_value"):
+                 "xy_value", "nan3", "tabulated3", "regions5", "subregions5x5_peak2", "predict_split_peak2",
+                 "predict_split_snapshot", "mcubes_gauss3", "quad_mcubes_gauss3", "mcubes_value"):
         assert case in names, case

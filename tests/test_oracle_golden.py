@@ -145,3 +145,26 @@ def test_canonical_sum_is_compensated(orc):
     rng = np.random.default_rng(3)
     y = rng.standard_normal(50000)
     assert abs(orc.canon_sum(y) - math.fsum(y)) <= 1e-12 * np.abs(y).sum()
+
+
+def test_oracle_regions_entry_equals_plain(orc):
+    """The oracle's first-list entry with no list is its plain integrate."""
+    import gpuintegration_gb300 as pg
+    for fam, d in ((pg.PRODUCT_PEAK, 3), (pg.CORNER_PEAK, 4)):
+        f = pg.genz(fam, [4.0] * d, [0.3] * d)
+        a, _ = orc.integrate(f, 1e-5, 0.0)
+        b, _ = orc.integrate_regions(f, None, None, 1e-5, 0.0)
+        assert (a.estimate, a.errorest, a.nregions, a.iters) == (b.estimate, b.errorest, b.nregions, b.iters)
+
+
+def test_oracle_predict_split_keeps_iteration_15(orc):
+    """predict_split (Workspace.cuh:415-441): with classification off for 15
+    iterations every region splits, so the list of iteration 15 of a 2-D run
+    holds 16 * 2^15 regions covering the unit square."""
+    import numpy as np
+    import gpuintegration_gb300 as pg
+    f = pg.genz(pg.GAUSSIAN, [20.0, 20.0], [0.37, 0.61])
+    r, snap = orc.integrate_regions(f, None, None, 1e-12, 0.0, predict_split=True, snap_cap=1 << 20)
+    assert r.status == 0 and snap[0] == 16 * 2 ** 15
+    left, length = snap[1]
+    assert abs(np.prod(length, axis=0).sum() - 1.0) < 1e-12
