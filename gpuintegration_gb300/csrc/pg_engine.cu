@@ -145,7 +145,7 @@ Engine::Engine(int dev) : device(dev) {}
 
 Engine::~Engine() {
   cudaSetDevice(device);
-  DevBuf* dev_bufs[] = {&rule_trie_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
+  DevBuf* dev_bufs[] = {&rule_trie_, &rule_leafset_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
                         &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
                         &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
                         &thr_out_, &adm_starts_, &adm_ids_, &sp_left_, &sp_len_, &sp_par_};
@@ -295,11 +295,16 @@ int Engine::init(std::string* why) {
   }
   code_coefficients(r2, R.A, R.B);
   std::vector<uint16_t> tries;
+  std::vector<uint32_t> leafset;
   for (int d = PG_MIN_NDIM; d <= kTrieMaxDim; ++d) {
     RuleTable t = make_rule(d);
     R.trie_off[d] = (int32_t)tries.size();
     std::vector<uint16_t> tv = prefix_trie(t);
     tries.insert(tries.end(), tv.begin(), tv.end());
+    // the last t.feval entries are the leaves, in point order
+    R.leafset_off[d] = (int32_t)leafset.size();
+    for (int p = 0; p < t.feval; ++p)
+      leafset.push_back((uint32_t)tv[tv.size() - t.feval + p] | ((uint32_t)(t.code[p] >> 60) << 16));
   }
   const double q = r2.G[1] / r2.G[0];
   R.ratio = q * q;
@@ -322,6 +327,12 @@ int Engine::init(std::string* why) {
     return rc;
   }
   PG_INIT_TRY(cudaMemcpy(rule_trie_.p, tries.data(), tries.size() * 2, cudaMemcpyHostToDevice), "rule upload");
+  if ((rc = ensure(rule_leafset_, leafset.size() * 4)) != PG_OK) {
+    if (why) *why = last_error;
+    return rc;
+  }
+  PG_INIT_TRY(cudaMemcpy(rule_leafset_.p, leafset.data(), leafset.size() * 4, cudaMemcpyHostToDevice), "rule upload");
+  R.leafset = (const uint32_t*)rule_leafset_.p;
   R.trie = (const uint16_t*)rule_trie_.p;
   R.code = (const uint64_t*)rule_code_.p;
   R.w = (const double*)rule_w_.p;

@@ -224,7 +224,7 @@ class Engine {
 
   cudaStream_t stream_ = nullptr;
   RuleDev rule_{};
-  DevBuf rule_code_, rule_w_, rule_scale_, rule_norm_, rule_trie_;
+  DevBuf rule_code_, rule_w_, rule_scale_, rule_norm_, rule_trie_, rule_leafset_;
   // region lists (ping-pong) and owners
   DevBuf left_[2], len_[2], owner_[2], parent_[2];
   uint64_t reg_cap_[2] = {0, 0};

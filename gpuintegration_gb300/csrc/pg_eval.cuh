@@ -21,6 +21,10 @@ struct RuleDev {
   const uint64_t* code;             // packed points, concatenated over ndim
   const uint16_t* trie;             // prefix tries (pg_rule.h), concatenated over ndim <= kTrieMaxDim
   int32_t trie_off[kMaxNdim + 1];
+  // Per point of the ndim <= kTrieMaxDim rules: the trie leaf entry (parent
+  // index | last-axis code << 12) | the point's generator set << 16.
+  const uint32_t* leafset;
+  int32_t leafset_off[kMaxNdim + 1];
   const double* w;                  // [(kMaxNdim + 1) * 45]
   const double* scale;
   const double* norm;
@@ -44,6 +48,7 @@ struct RuleDev {
 // Trie buffers of the d <= 8 kernel: depth d-1 (at most feval(7) = 717 nodes)
 // and depth d-2 (at most feval(6) = 453), alternating downwards.
 constexpr int kTrieMaxDim = 8;
+constexpr int kWStride = 6;  // padded row of the 5 rule weights of a generator set
 constexpr int kTrieBufA = 720, kTrieBufB = 456;
 
 template <int MAXD>
@@ -63,7 +68,7 @@ struct EvalWarpSmem {
   double fv[64];
   double lo[MAXD];
   double up[MAXD];
-  double w[kNSets * kNRules];
+  alignas(16) double w[kNSets * kWStride];  // weights of set s at [s * kWStride, +5), 16-byte aligned rows
   double scale[kNSets * kNRules];
   double norm[kNSets * kNRules];
 };
@@ -87,24 +92,29 @@ constexpr int kPointsTrie = 0, kPointsProduct = 1, kPointsEval = 2;
 template <int MAXD, int MODE, bool SCALE, class Fn>
 __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, const Fn& fn,
                                            const uint64_t* __restrict__ codes, int feval, int d, int lane,
-                                           const uint16_t* __restrict__ leaf_tab, const double* leaf_src,
+                                           const uint32_t* __restrict__ leafset, const double* leaf_src,
                                            const double* leaf_fac, double jac) {
   for (int base = 0; base < feval; base += 64) {
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       const int p = base + half * 32 + lane;
       if (p < feval) {
-        const uint64_t code = __ldg(&codes[p]);
         double f;
+        int set;
         if constexpr (MODE == kPointsTrie) {
-          const uint32_t e = __ldg(&leaf_tab[p]);
-          f = __dmul_rn(leaf_src[e & 0xfffu], leaf_fac[e >> 12]);
+          const uint32_t e = __ldg(&leafset[p]);
+          f = __dmul_rn(leaf_src[e & 0xfffu], leaf_fac[(e >> 12) & 15u]);
+          set = (int)(e >> 16);
         } else if constexpr (MODE == kPointsProduct) {
+          const uint64_t code = __ldg(&codes[p]);
+          set = (int)(code >> 60);
           f = S.fac[(int)(code & 15u)];
 #pragma unroll
           for (int k = 1; k < MAXD; ++k)
             if (k < d) f = __dmul_rn(f, S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)]);
         } else {
+          const uint64_t code = __ldg(&codes[p]);
+          set = (int)(code >> 60);
           double x[MAXD];
 #pragma unroll
           for (int k = 0; k < MAXD; ++k)
@@ -113,19 +123,22 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
         }
         if constexpr (SCALE) f = __dmul_rn(f, jac);
         if (base == 0) S.fv[p] = f;
-        const double* w = &S.w[(int)(code >> 60) * kNRules];
+        const double* wr = &S.w[set * kWStride];
+        const double2 w01 = *reinterpret_cast<const double2*>(wr);
+        const double2 w23 = *reinterpret_cast<const double2*>(wr + 2);
+        const double w4 = wr[4];
         if (half == 0) {
-          rs.a0 = __fma_rn(f, w[0], rs.a0);
-          rs.a1 = __fma_rn(f, w[1], rs.a1);
-          rs.a2 = __fma_rn(f, w[2], rs.a2);
-          rs.a3 = __fma_rn(f, w[3], rs.a3);
-          rs.a4 = __fma_rn(f, w[4], rs.a4);
+          rs.a0 = __fma_rn(f, w01.x, rs.a0);
+          rs.a1 = __fma_rn(f, w01.y, rs.a1);
+          rs.a2 = __fma_rn(f, w23.x, rs.a2);
+          rs.a3 = __fma_rn(f, w23.y, rs.a3);
+          rs.a4 = __fma_rn(f, w4, rs.a4);
         } else {
-          rs.b0 = __fma_rn(f, w[0], rs.b0);
-          rs.b1 = __fma_rn(f, w[1], rs.b1);
-          rs.b2 = __fma_rn(f, w[2], rs.b2);
-          rs.b3 = __fma_rn(f, w[3], rs.b3);
-          rs.b4 = __fma_rn(f, w[4], rs.b4);
+          rs.b0 = __fma_rn(f, w01.x, rs.b0);
+          rs.b1 = __fma_rn(f, w01.y, rs.b1);
+          rs.b2 = __fma_rn(f, w23.x, rs.b2);
+          rs.b3 = __fma_rn(f, w23.y, rs.b3);
+          rs.b4 = __fma_rn(f, w4, rs.b4);
         }
       }
     }
@@ -133,7 +146,7 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
 }
 
 template <int MAXD, int WARPS, class Fn>
-static __global__ void __launch_bounds__(WARPS * 32)
+static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     eval_kernel(const double* __restrict__ left, const double* __restrict__ length, uint64_t n, uint64_t stride,
                 const uint32_t* __restrict__ owner, const IntegralDesc* __restrict__ descs, RuleDev rule, Fn fn,
                 double* __restrict__ est, double* __restrict__ err, int32_t* __restrict__ bisect) {
@@ -157,10 +170,11 @@ static __global__ void __launch_bounds__(WARPS * 32)
       feval = rule.feval[d];
       codes = rule.code + rule.code_off[d];
       for (int q = lane; q < kNSets * kNRules; q += 32) {
-        S.w[q] = rule.w[d * 45 + q];
+        S.w[(q / kNRules) * kWStride + q % kNRules] = rule.w[d * 45 + q];
         S.scale[q] = rule.scale[d * 45 + q];
         S.norm[q] = rule.norm[d * 45 + q];
       }
+      if (lane < kNSets) S.w[lane * kWStride + kNRules] = 0.0;
       cur = j;
       __syncwarp();
     }
@@ -186,7 +200,7 @@ static __global__ void __launch_bounds__(WARPS * 32)
     // goes to buffer a when d-1-k is even, else b; depth 1 is the axis-0
     // factor row).  Depth d is formed point by point below.
     const double* leaf_src = S.fac;
-    const uint16_t* leaf_tab = nullptr;
+    const uint32_t* leafset = nullptr;
     if constexpr (MAXD <= kTrieMaxDim) {
       if (sep) {
         const uint16_t* tt = rule.trie + rule.trie_off[d];
@@ -204,7 +218,7 @@ static __global__ void __launch_bounds__(WARPS * 32)
           __syncwarp();
         }
         leaf_src = (d == 2) ? S.fac : S.trie.a;
-        leaf_tab = tt + off;
+        leafset = rule.leafset + rule.leafset_off[d];
       }
     }
     const double* leaf_fac = S.fac + (d - 1) * kCodesPerDim;
@@ -213,21 +227,21 @@ static __global__ void __launch_bounds__(WARPS * 32)
     // per-point instruction is spent on either decision.
     const double jac = S.desc.jac;
     RuleSums rs{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const int mode = (sep && leaf_tab) ? kPointsTrie : (sep ? kPointsProduct : kPointsEval);
+    const int mode = (sep && leafset) ? kPointsTrie : (sep ? kPointsProduct : kPointsEval);
     if (jac != 1.0) {
       if (mode == kPointsTrie)
-        point_sums<MAXD, kPointsTrie, true>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsTrie, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
       else if (mode == kPointsProduct)
-        point_sums<MAXD, kPointsProduct, true>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsProduct, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
       else
-        point_sums<MAXD, kPointsEval, true>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsEval, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
     } else {
       if (mode == kPointsTrie)
-        point_sums<MAXD, kPointsTrie, false>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsTrie, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
       else if (mode == kPointsProduct)
-        point_sums<MAXD, kPointsProduct, false>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsProduct, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
       else
-        point_sums<MAXD, kPointsEval, false>(rs, S, fn, codes, feval, d, lane, leaf_tab, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsEval, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
     }
     // The reference's block sum (Sample.cuh:49-83) per rule: a shuffle-down
     // tree over each 32-lane half (offsets 16, 8, 4, 2, 1), then
