@@ -298,13 +298,13 @@ int Engine::init(std::string* why) {
   std::vector<uint32_t> leafset;
   for (int d = PG_MIN_NDIM; d <= kTrieMaxDim; ++d) {
     RuleTable t = make_rule(d);
+    std::vector<uint16_t> inner;
+    std::vector<uint32_t> leaf;
+    split_trie(t, &inner, &leaf);
     R.trie_off[d] = (int32_t)tries.size();
-    std::vector<uint16_t> tv = prefix_trie(t);
-    tries.insert(tries.end(), tv.begin(), tv.end());
-    // the last t.feval entries are the leaves, in point order
+    tries.insert(tries.end(), inner.begin(), inner.end());
     R.leafset_off[d] = (int32_t)leafset.size();
-    for (int p = 0; p < t.feval; ++p)
-      leafset.push_back((uint32_t)tv[tv.size() - t.feval + p] | ((uint32_t)(t.code[p] >> 60) << 16));
+    leafset.insert(leafset.end(), leaf.begin(), leaf.end());
   }
   const double q = r2.G[1] / r2.G[0];
   R.ratio = q * q;

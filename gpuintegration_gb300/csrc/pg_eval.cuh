@@ -19,10 +19,10 @@ namespace pg {
 // Rule tables for every ndim, in device memory; passed by value.
 struct RuleDev {
   const uint64_t* code;             // packed points, concatenated over ndim
-  const uint16_t* trie;             // prefix tries (pg_rule.h), concatenated over ndim <= kTrieMaxDim
-  int32_t trie_off[kMaxNdim + 1];
-  // Per point of the ndim <= kTrieMaxDim rules: the trie leaf entry (parent
-  // index | last-axis code << 12) | the point's generator set << 16.
+  const uint16_t* trie;             // inner entries of the half tries (split_trie in pg_rule.h),
+  int32_t trie_off[kMaxNdim + 1];   // concatenated over ndim <= kTrieMaxDim
+  // Per point of the ndim <= kTrieMaxDim rules: left node | right node << 8 |
+  // generator set << 16.
   const uint32_t* leafset;
   int32_t leafset_off[kMaxNdim + 1];
   const double* w;                  // [(kMaxNdim + 1) * 45]
@@ -45,16 +45,18 @@ struct RuleDev {
 // tree per 32-lane half, then (half0 + 0) + half1.  Each per-axis coordinate
 // value a region can take (centre, +-G0..G4) is computed once per region.
 // ---------------------------------------------------------------------------
-// Trie buffers of the d <= 8 kernel: depth d-1 (at most feval(7) = 717 nodes)
-// and depth d-2 (at most feval(6) = 453), alternating downwards.
+// Half-trie buffers of the d <= 8 kernel: per half, the depth-2 and depth-4
+// nodes (at most feval(4) = 153) share one buffer and the depth-3 nodes (at
+// most feval(3) = 77) use the other.  The area also holds the reduction trees
+// (325 doubles).
 constexpr int kTrieMaxDim = 8;
 constexpr int kWStride = 6;  // padded row of the 5 rule weights of a generator set
-constexpr int kTrieBufA = 720, kTrieBufB = 456;
+constexpr int kHalfEven = 160, kHalfOdd = 80;
+constexpr int kTrieBuf = 2 * (kHalfEven + kHalfOdd);
 
 template <int MAXD>
 struct EvalTrieSmem {
-  double a[kTrieBufA];
-  double b[kTrieBufB];
+  double a[kTrieBuf];  // left even | left odd | right even | right odd
 };
 template <>
 struct EvalTrieSmem<16> {};
@@ -92,8 +94,8 @@ constexpr int kPointsTrie = 0, kPointsProduct = 1, kPointsEval = 2;
 template <int MAXD, int MODE, bool SCALE, class Fn>
 __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, const Fn& fn,
                                            const uint64_t* __restrict__ codes, int feval, int d, int lane,
-                                           const uint32_t* __restrict__ leafset, const double* leaf_src,
-                                           const double* leaf_fac, double jac) {
+                                           const uint32_t* __restrict__ leafset, const double* leaf_l,
+                                           const double* leaf_r, double jac) {
   for (int base = 0; base < feval; base += 64) {
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -103,15 +105,22 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
         int set;
         if constexpr (MODE == kPointsTrie) {
           const uint32_t e = __ldg(&leafset[p]);
-          f = __dmul_rn(leaf_src[e & 0xfffu], leaf_fac[(e >> 12) & 15u]);
+          f = __dmul_rn(leaf_l[e & 0xffu], leaf_r[(e >> 8) & 0xffu]);
           set = (int)(e >> 16);
         } else if constexpr (MODE == kPointsProduct) {
           const uint64_t code = __ldg(&codes[p]);
           set = (int)(code >> 60);
-          f = S.fac[(int)(code & 15u)];
+          // L * R (m = d / 2), each half in axis order
+          const int m = d / 2;
+          double L = S.fac[(int)(code & 15u)];
+          double R = S.fac[m * kCodesPerDim + (int)((code >> (4 * m)) & 15u)];
 #pragma unroll
-          for (int k = 1; k < MAXD; ++k)
-            if (k < d) f = __dmul_rn(f, S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)]);
+          for (int k = 1; k < MAXD; ++k) {
+            const double h = S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)];
+            if (k < m) L = __dmul_rn(L, h);
+            else if (k > m && k < d) R = __dmul_rn(R, h);
+          }
+          f = __dmul_rn(L, R);
         } else {
           const uint64_t code = __ldg(&codes[p]);
           set = (int)(code >> 60);
@@ -196,32 +205,42 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     if (sep)
       for (int v = lane; v < d * kCodesPerDim; v += 32) S.fac[v] = fn.factor(S.desc, v / kCodesPerDim, S.tab[v]);
     __syncwarp();
-    // Product-form integrands with d <= 8: inner trie depths 2..d-1 (depth k
-    // goes to buffer a when d-1-k is even, else b; depth 1 is the axis-0
-    // factor row).  Depth d is formed point by point below.
-    const double* leaf_src = S.fac;
+    // Product-form integrands with d <= 8: the half products L (axes 0..m-1)
+    // and R (axes m..d-1), depth by depth, both halves' nodes of a depth in
+    // the same warp instructions (depth 1 is the factor row of the half's
+    // first axis).  Each point then takes one multiply, L * R.
+    const double* leaf_l = S.fac;
+    const double* leaf_r = S.fac;
     const uint32_t* leafset = nullptr;
     if constexpr (MAXD <= kTrieMaxDim) {
       if (sep) {
         const uint16_t* tt = rule.trie + rule.trie_off[d];
+        const int m = d / 2, mr = d - m;
+        double* const lb[2] = {S.trie.a, S.trie.a + kHalfEven};
+        double* const rb[2] = {S.trie.a + kHalfEven + kHalfOdd, S.trie.a + 2 * kHalfEven + kHalfOdd};
         int off = 0;
-        for (int k = 2; k <= d - 1; ++k) {
-          const int m = rule.feval[k];
-          const double* src = (k - 1 == 1) ? S.fac : (((d - 1 - (k - 1)) & 1) ? S.trie.b : S.trie.a);
-          double* dst = ((d - 1 - k) & 1) ? S.trie.b : S.trie.a;
-          const double* fk = S.fac + (k - 1) * kCodesPerDim;
-          for (int i = lane; i < m; i += 32) {
+        for (int k = 2; k <= mr; ++k) {  // mr >= m
+          const int nl = (k <= m) ? rule.feval[k] : 0, nr = rule.feval[k];
+          const double* srcl = (k == 2) ? S.fac : lb[(k - 1) & 1];
+          const double* srcr = (k == 2) ? S.fac + m * kCodesPerDim : rb[(k - 1) & 1];
+          const double* fl = S.fac + (k - 1) * kCodesPerDim;
+          const double* fr = S.fac + (m + k - 1) * kCodesPerDim;
+          for (int i = lane; i < nl + nr; i += 32) {
             const uint32_t e = __ldg(&tt[off + i]);
-            dst[i] = __dmul_rn(src[e & 0xfffu], fk[e >> 12]);
+            const bool left = i < nl;
+            const double* src = left ? srcl : srcr;
+            const double* fk = left ? fl : fr;
+            double* dst = left ? lb[k & 1] + i : rb[k & 1] + (i - nl);
+            *dst = __dmul_rn(src[e & 0xfffu], fk[e >> 12]);
           }
-          off += m;
+          off += nl + nr;
           __syncwarp();
         }
-        leaf_src = (d == 2) ? S.fac : S.trie.a;
+        leaf_l = (m == 1) ? S.fac : lb[m & 1];
+        leaf_r = (mr == 1) ? S.fac + m * kCodesPerDim : rb[mr & 1];
         leafset = rule.leafset + rule.leafset_off[d];
       }
     }
-    const double* leaf_fac = S.fac + (d - 1) * kCodesPerDim;
     // The per-point loop, specialised on how f is formed and on whether the
     // box's Jacobian differs from 1 (both uniform over the region), so no
     // per-point instruction is spent on either decision.
@@ -230,18 +249,18 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     const int mode = (sep && leafset) ? kPointsTrie : (sep ? kPointsProduct : kPointsEval);
     if (jac != 1.0) {
       if (mode == kPointsTrie)
-        point_sums<MAXD, kPointsTrie, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsTrie, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
       else if (mode == kPointsProduct)
-        point_sums<MAXD, kPointsProduct, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsProduct, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
       else
-        point_sums<MAXD, kPointsEval, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsEval, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
     } else {
       if (mode == kPointsTrie)
-        point_sums<MAXD, kPointsTrie, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsTrie, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
       else if (mode == kPointsProduct)
-        point_sums<MAXD, kPointsProduct, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsProduct, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
       else
-        point_sums<MAXD, kPointsEval, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_src, leaf_fac, jac);
+        point_sums<MAXD, kPointsEval, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
     }
     // The reference's block sum (Sample.cuh:49-83) per rule: a shuffle-down
     // tree over each 32-lane half (offsets 16, 8, 4, 2, 1), then

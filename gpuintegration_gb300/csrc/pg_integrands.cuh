@@ -56,10 +56,14 @@ __device__ __forceinline__ double ipow_dev(double s, int e) {
   return r;
 }
 
-// Families that are products of per-axis factors h_k(x_k).  A region's
+// Families that are products of per-axis factors h_k(x_k).  The product is
+// taken in two halves, f = L * R, L = h_0 * h_1 * ... * h_{m-1} and
+// R = h_m * ... * h_{d-1} (m = d / 2), each half in axis order.  A region's
 // points take only 11 coordinate values per axis, so the evaluation kernel
-// computes each factor once per region and forms every point's value as the
-// product of its axes' factors (same operations, same order, same value).
+// computes each factor once per region, the distinct half products once per
+// region (prefix tries of the two halves), and each point's value with one
+// multiply (same operations, same order, same value as this definition).
+__host__ __device__ __forceinline__ int product_split(int d) { return d / 2; }
 __host__ __device__ __forceinline__ bool family_separable(int family) {
   return family == FAM_PRODUCT_PEAK || family == FAM_GAUSSIAN || family == FAM_C0 || family == FAM_DISCONTINUOUS ||
          family == FAM_PRODUCT;
@@ -86,6 +90,21 @@ __device__ __forceinline__ double family_factor(const IntegralDesc& D, int k, do
   return 1.0;
 }
 
+// L * R of the product-form families (factors, or the coordinates themselves
+// for PRODUCT).
+template <int MAXD>
+__device__ __forceinline__ double split_product(const IntegralDesc& D, const double* x, bool factors) {
+  const int d = D.d, m = product_split(d);
+  double L = factors ? family_factor(D, 0, x[0]) : x[0];
+  double R = factors ? family_factor(D, m, x[m]) : x[m];
+#pragma unroll
+  for (int i = 1; i < MAXD; ++i) {
+    if (i < m) L = __dmul_rn(L, factors ? family_factor(D, i, x[i]) : x[i]);
+    else if (i > m && i < d) R = __dmul_rn(R, factors ? family_factor(D, i, x[i]) : x[i]);
+  }
+  return __dmul_rn(L, R);
+}
+
 template <int MAXD>
 __device__ __forceinline__ double family_eval(const IntegralDesc& D, const double* x) {
   const int d = D.d;
@@ -99,13 +118,8 @@ __device__ __forceinline__ double family_eval(const IntegralDesc& D, const doubl
         if (i < d) s = __fma_rn(D.a[i], x[i], s);
       return cos(s);
     }
-    case FAM_PRODUCT_PEAK: {
-      double v = family_factor(D, 0, x[0]);
-#pragma unroll
-      for (int i = 1; i < MAXD; ++i)
-        if (i < d) v = __dmul_rn(v, family_factor(D, i, x[i]));
-      return v;
-    }
+    case FAM_PRODUCT_PEAK:
+      return split_product<MAXD>(D, x, true);
     case FAM_CORNER_PEAK: {
       double s = 1.0;
 #pragma unroll
@@ -115,21 +129,10 @@ __device__ __forceinline__ double family_eval(const IntegralDesc& D, const doubl
     }
     case FAM_GAUSSIAN:
     case FAM_C0:
-    case FAM_DISCONTINUOUS: {
-      // Product of per-axis factors, axis 0 first.
-      double v = family_factor(D, 0, x[0]);
-#pragma unroll
-      for (int i = 1; i < MAXD; ++i)
-        if (i < d) v = __dmul_rn(v, family_factor(D, i, x[i]));
-      return v;
-    }
-    case FAM_PRODUCT: {
-      double v = x[0];
-#pragma unroll
-      for (int i = 1; i < MAXD; ++i)
-        if (i < d) v = __dmul_rn(v, x[i]);
-      return v;
-    }
+    case FAM_DISCONTINUOUS:
+      return split_product<MAXD>(D, x, true);
+    case FAM_PRODUCT:
+      return split_product<MAXD>(D, x, false);
     case FAM_NAN:
       return __longlong_as_double(0x7ff8000000000000LL);
     case FAM_BOX: {

@@ -1,5 +1,6 @@
 // Degree-9 rule tables (library side).  Compiled with -ffp-contract=off so the
 // weight polynomials round exactly as the reference's host code does on x86-64.
+#include <map>
 #include "pg_rule.h"
 
 #include <algorithm>
@@ -198,37 +199,46 @@ RuleTable make_rule(int d) {
   return r;
 }
 
-std::vector<uint16_t> prefix_trie(const RuleTable& r) {
-  const int d = r.ndim;
-  std::vector<std::vector<uint8_t>> pts(r.feval, std::vector<uint8_t>(d));
-  for (int p = 0; p < r.feval; ++p)
-    for (int k = 0; k < d; ++k) pts[p][k] = (uint8_t)((r.code[p] >> (4 * k)) & 15u);
-  // levels[k]: node prefixes of depth k (k = 1..d)
-  std::vector<std::vector<std::vector<uint8_t>>> levels(d + 1);
-  std::vector<std::vector<uint16_t>> entries(d + 1);
-  levels[d] = pts;
-  for (int k = d; k >= 2; --k) {
-    std::vector<std::vector<uint8_t>>& up = levels[k - 1];
-    for (const auto& node : levels[k]) {
-      std::vector<uint8_t> pre(node.begin(), node.begin() + (k - 1));
-      int idx;
-      if (k - 1 == 1) {
-        idx = pre[0];
+// Distinct code prefixes of the axes [a, a + m) in order of first appearance
+// over the points; returns per point its node index at depth m and appends
+// the entries of depths 2..m to levels[k].
+static std::vector<int> half_trie(const RuleTable& r, int a, int m, std::vector<std::vector<uint16_t>>* levels) {
+  const int np = r.feval;
+  std::vector<int> node(np);
+  for (int p = 0; p < np; ++p) node[p] = (int)((r.code[p] >> (4 * a)) & 15u);  // depth 1: the code
+  for (int k = 2; k <= m; ++k) {
+    std::map<std::pair<int, int>, int> index;  // (parent, code) -> node at depth k
+    for (int p = 0; p < np; ++p) {
+      const int c = (int)((r.code[p] >> (4 * (a + k - 1))) & 15u);
+      const auto key = std::make_pair(node[p], c);
+      auto it = index.find(key);
+      int id;
+      if (it == index.end()) {
+        id = (int)index.size();
+        index.emplace(key, id);
+        (*levels)[k].push_back((uint16_t)(node[p] | (c << 12)));
       } else {
-        auto it = std::find(up.begin(), up.end(), pre);
-        if (it == up.end()) {
-          up.push_back(pre);
-          idx = (int)up.size() - 1;
-        } else {
-          idx = (int)(it - up.begin());
-        }
+        id = it->second;
       }
-      entries[k].push_back((uint16_t)(idx | ((int)node[k - 1] << 12)));
+      node[p] = id;
     }
   }
-  std::vector<uint16_t> out;
-  for (int k = 2; k <= d; ++k) out.insert(out.end(), entries[k].begin(), entries[k].end());
-  return out;
+  return node;
+}
+
+void split_trie(const RuleTable& r, std::vector<uint16_t>* inner, std::vector<uint32_t>* leaf) {
+  const int d = r.ndim, m = d / 2;
+  std::vector<std::vector<uint16_t>> lv(d + 1), rv(d + 1);
+  const std::vector<int> ln = half_trie(r, 0, m, &lv);
+  const std::vector<int> rn = half_trie(r, m, d - m, &rv);
+  inner->clear();
+  for (int k = 2; k <= std::max(m, d - m); ++k) {
+    if (k <= m) inner->insert(inner->end(), lv[k].begin(), lv[k].end());
+    if (k <= d - m) inner->insert(inner->end(), rv[k].begin(), rv[k].end());
+  }
+  leaf->resize(r.feval);
+  for (int p = 0; p < r.feval; ++p)
+    (*leaf)[p] = (uint32_t)ln[p] | ((uint32_t)rn[p] << 8) | ((uint32_t)(r.code[p] >> 60) << 16);
 }
 
 void code_coefficients(const RuleTable& r, double* A, double* B) {

@@ -32,15 +32,20 @@ struct RuleTable {
 int feval_count(int ndim);
 RuleTable make_rule(int ndim);
 
-// Prefix trie of the points' per-axis codes, for integrands that are a
-// left-to-right product of per-axis factors: a depth-k node is a distinct
-// prefix (c_0..c_{k-1}); its value is its parent's value times the factor of
-// axis k-1 at code c_{k-1}, so every point's product is formed with exactly
-// the roundings of v = f_0 * f_1 * ... * f_{d-1}, sharing common prefixes.
-// Depth-1 node i is code i.  Entries for depths 2..d follow each other; entry
-// = parent index (12 bits) | code << 12; depth d lists the points in rule
-// order.  Depth k has feval_count(k) nodes (feval_count(1) = 11).
-std::vector<uint16_t> prefix_trie(const RuleTable& r);
+// Prefix tries of the two halves of the points' per-axis codes, for
+// integrands f = L * R with L the product of the factors of axes 0..m-1 and R
+// that of axes m..d-1 (m = d / 2), each half in axis order.  In a half
+// starting at axis a, a depth-k node is a distinct code prefix
+// (c_a..c_{a+k-1}); its value is its parent's value times the factor of axis
+// a+k-1 at code c_{a+k-1}, so each half product is formed with exactly the
+// roundings of the definition, once per distinct prefix.  Depth-1 node i is
+// code i.  `inner` lists, for depth k = 2, 3, ...: the left half's depth-k
+// entries (while k <= m), then the right half's (while k <= d - m); entry =
+// parent index (12 bits) | code << 12.  `leaf` gives per point, in rule
+// order: left node index at depth m | right node index at depth d - m << 8 |
+// generator set << 16.  A half of k axes has feval_count(k) nodes at depth k
+// (feval_count(1) = 11).
+void split_trie(const RuleTable& r, std::vector<uint16_t>* inner, std::vector<uint32_t>* leaf);
 
 // A = .5 + g and B = .5 - g for the 11 coordinate codes, as the reference
 // computes them per point (Sample.cuh:126-130).

@@ -54,7 +54,12 @@ typedef enum pg_status {
  *   PRODUCT         prod x_i                           (test/cuda/pagani/do_integration_from_c.cu:7-14)
  *   NAN_VALUE       NaN                                (test/cuda/pagani/NanIntegral.cu:9-16)
  *   BOX             (sum x_i^2)^(c/2)                  (cuda/pagani/demos/function.cuh:113-172)
- *   FUN6            6-D test function of test/cuda/pagani/accuracy_improves_with_epsrel.cu:17-27 */
+ *   FUN6            6-D test function of test/cuda/pagani/accuracy_improves_with_epsrel.cu:17-27
+ * The product-form families (PRODUCT_PEAK, GAUSSIAN, C0, DISCONTINUOUS,
+ * PRODUCT) are evaluated as a product of per-axis factors h_i taken in two
+ * halves, (h_0 * ... * h_{m-1}) * (h_m * ... * h_{d-1}) with m = ndim / 2, each
+ * half in axis order; a caller who needs another order passes a functor
+ * through the C++ layer (pagani_gb300.cuh). */
 typedef enum pg_family {
   PG_FAMILY_CONSTANT = 0,
   PG_FAMILY_OSCILLATORY = 1,

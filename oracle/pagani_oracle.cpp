@@ -129,10 +129,13 @@ static double eval(const Prepared& p, const double* x) {
     case FAM_GAUSSIAN:
     case FAM_C0:
     case FAM_DISCONTINUOUS: {
-      // Product of per-axis factors, axis 0 first.
-      double v = factor(p, 0, x[0]);
-      for (int i = 1; i < d; ++i) v = v * factor(p, i, x[i]);
-      return v;
+      // f = L * R: products of the per-axis factors of axes 0..m-1 and
+      // m..d-1 (m = d / 2), each half in axis order.
+      const int m = d / 2;
+      double L = factor(p, 0, x[0]), R = factor(p, m, x[m]);
+      for (int i = 1; i < m; ++i) L = L * factor(p, i, x[i]);
+      for (int i = m + 1; i < d; ++i) R = R * factor(p, i, x[i]);
+      return L * R;
     }
     case FAM_CORNER_PEAK: {
       double s = 1.0;
@@ -140,9 +143,11 @@ static double eval(const Prepared& p, const double* x) {
       return 1.0 / ipow(s, d + 1);
     }
     case FAM_PRODUCT: {
-      double v = x[0];
-      for (int i = 1; i < d; ++i) v = v * x[i];
-      return v;
+      const int m = d / 2;
+      double L = x[0], R = x[m];
+      for (int i = 1; i < m; ++i) L = L * x[i];
+      for (int i = m + 1; i < d; ++i) R = R * x[i];
+      return L * R;
     }
     case FAM_NAN:
       return std::numeric_limits<double>::quiet_NaN();

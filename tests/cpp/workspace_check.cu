@@ -15,20 +15,29 @@
 
 #include "pagani_gb300.cuh"
 
-// exp(-(a_k (x_k - u_k))^2) per axis, product in axis order (the GAUSSIAN family, c = 0).
+// The library's product-form families multiply their per-axis factors in two
+// halves: f = L * R, L over axes 0..m-1 and R over m..d-1 (m = d / 2), each in
+// axis order.
+template <int ND, class H>
+__device__ double split_product(const double* x, const H& h) {
+  constexpr int m = ND / 2;
+  double L = h(0, x[0]), R = h(m, x[m]);
+  for (int k = 1; k < m; ++k) L = __dmul_rn(L, h(k, x[k]));
+  for (int k = m + 1; k < ND; ++k) R = __dmul_rn(R, h(k, x[k]));
+  return __dmul_rn(L, R);
+}
+
+// exp(-(a_k (x_k - u_k))^2) per axis (the GAUSSIAN family, c = 0).
 template <int ND>
 struct GaussProduct {
   double a[ND], u[ND];
   template <class... X>
   __device__ double operator()(X... xs) const {
     const double x[ND] = {static_cast<double>(xs)...};
-    double v = 1.0;
-    for (int k = 0; k < ND; ++k) {
-      const double q = __dmul_rn(a[k], __dsub_rn(x[k], u[k]));
-      const double h = exp(-__dmul_rn(q, q));
-      v = (k == 0) ? h : __dmul_rn(v, h);
-    }
-    return v;
+    return split_product<ND>(x, [this](int k, double xk) {
+      const double q = __dmul_rn(a[k], __dsub_rn(xk, u[k]));
+      return exp(-__dmul_rn(q, q));
+    });
   }
 };
 
@@ -39,13 +48,10 @@ struct PeakProduct {
   template <class... X>
   __device__ double operator()(X... xs) const {
     const double x[ND] = {static_cast<double>(xs)...};
-    double v = 1.0;
-    for (int k = 0; k < ND; ++k) {
-      const double t = __dsub_rn(x[k], u[k]);
-      const double h = __ddiv_rn(1.0, __fma_rn(t, t, ia2[k]));
-      v = (k == 0) ? h : __dmul_rn(v, h);
-    }
-    return v;
+    return split_product<ND>(x, [this](int k, double xk) {
+      const double t = __dsub_rn(xk, u[k]);
+      return __ddiv_rn(1.0, __fma_rn(t, t, ia2[k]));
+    });
   }
 };
 
@@ -55,13 +61,10 @@ struct Gauss3c {
   double a, u, c;
   __device__ double operator()(double x, double y, double z) const {
     const double xs[3] = {x, y, z};
-    double v = 1.0;
-    for (int k = 0; k < 3; ++k) {
-      const double q = __dmul_rn(a, __dsub_rn(xs[k], u));
-      const double h = __dmul_rn(exp(-__dmul_rn(q, q)), c);
-      v = (k == 0) ? h : __dmul_rn(v, h);
-    }
-    return v;
+    return split_product<3>(xs, [this](int, double xk) {
+      const double q = __dmul_rn(a, __dsub_rn(xk, u));
+      return __dmul_rn(exp(-__dmul_rn(q, q)), c);
+    });
   }
 };
 
