@@ -18,13 +18,79 @@ constexpr int kNSets = 9;   // generator sets of the degree-9 rule (Rule.cuh:404
 constexpr int kMaxDim = 16;
 constexpr int kMaxNdim = 12;        // largest ndim the library instantiates tables for
 constexpr int kCodesPerDim = 11;    // 0, +G0..+G4, -G0..-G4
-constexpr int kEvalWarps = 8;       // warps (regions in flight) per evaluation CTA
 
 // Deterministic reduction geometry: chunk of 2048 elements, 256 threads x 8
 // items, item k of thread t is element chunk*2048 + k*256 + t.
 constexpr int kRedThreads = 256;
 constexpr int kRedItems = 8;
 constexpr int kChunk = kRedThreads * kRedItems;
+
+// ---------------------------------------------------------------------------
+// Double-precision multiply on the integer pipe.  GB300 executes FP64 at 2
+// lanes per SM per clock, which bounds region evaluation, while its integer
+// units run 32x wider.  mul_rn_int(a, b) returns exactly __dmul_rn(a, b)
+// (IEEE 754 binary64 product, round to nearest, ties to even): normal
+// operands with a normal product are multiplied in integer arithmetic (the
+// 106-bit product of the significands, normalised and rounded), a zero times
+// a finite value gives the signed zero, and every other case (subnormals,
+// infinities, NaNs, overflow, underflow) takes the FP64 multiply.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ unsigned long long mul_hi_u64(unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// Fast-path product; *ok is false when the operands need the FP64 multiply.
+__host__ __device__ __forceinline__ unsigned long long mul_rn_bits(unsigned long long A, unsigned long long B,
+                                                                   bool* ok) {
+  const unsigned long long sign = (A ^ B) & 0x8000000000000000ull;
+  const unsigned ea = (unsigned)(A >> 52) & 0x7ffu, eb = (unsigned)(B >> 52) & 0x7ffu;
+  const unsigned long long fa = A & 0x000fffffffffffffull, fb = B & 0x000fffffffffffffull;
+  const bool za = ea == 0 && fa == 0, zb = eb == 0 && fb == 0;
+  if ((za && eb != 0x7ffu) || (zb && ea != 0x7ffu)) {  // 0 * finite (either order)
+    *ok = true;
+    return sign;
+  }
+  int e = (int)ea + (int)eb - 1023;  // biased exponent of a product significand in [1, 2)
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u || e < 1 || e > 2046) {
+    *ok = false;
+    return 0;
+  }
+  const unsigned long long ma = fa | 0x0010000000000000ull, mb = fb | 0x0010000000000000ull;
+  const unsigned long long lo = ma * mb, hi = mul_hi_u64(ma, mb);  // P = hi * 2^64 + lo in [2^104, 2^106)
+  unsigned long long m, rest, half;
+  if (hi >> 41) {  // P >= 2^105
+    m = (hi << 11) | (lo >> 53);
+    rest = lo & 0x001fffffffffffffull;
+    half = 0x0010000000000000ull;
+    e += 1;
+  } else {
+    m = (hi << 12) | (lo >> 52);
+    rest = lo & 0x000fffffffffffffull;
+    half = 0x0008000000000000ull;
+  }
+  if (rest > half || (rest == half && (m & 1ull))) ++m;
+  if (m >> 53) {  // rounded up to 2^53
+    m >>= 1;
+    e += 1;
+  }
+  if (e > 2046) {
+    *ok = false;
+    return 0;
+  }
+  *ok = true;
+  return sign | ((unsigned long long)e << 52) | (m & 0x000fffffffffffffull);
+}
+
+__device__ __forceinline__ double mul_rn_int(double a, double b) {
+  bool ok;
+  const unsigned long long r =
+      mul_rn_bits((unsigned long long)__double_as_longlong(a), (unsigned long long)__double_as_longlong(b), &ok);
+  return ok ? __longlong_as_double((long long)r) : __dmul_rn(a, b);
+}
 
 // Neumaier-compensated pair (sum, correction).
 struct NS {

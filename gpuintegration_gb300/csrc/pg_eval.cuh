@@ -81,9 +81,10 @@ struct RuleSums {
   double a0, a1, a2, a3, a4, b0, b1, b2, b3, b4;
 };
 
-// How a point's value is formed: from the prefix trie of per-axis factors
-// (product-form integrands, d <= 8), as the left-to-right product of per-axis
-// factors, or by evaluating the integrand on the point's coordinates.
+// How a point's value is formed: from the half tries of per-axis factors
+// (product-form integrands, d <= 8: one multiply L * R), as the two-half
+// product of per-axis factors (product-form, d > 8), or by evaluating the
+// integrand on the point's coordinates.
 constexpr int kPointsTrie = 0, kPointsProduct = 1, kPointsEval = 2;
 
 // The per-point loop of eval_kernel: lane l takes points l, l+64, ... into a*
@@ -105,7 +106,7 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
         int set;
         if constexpr (MODE == kPointsTrie) {
           const uint32_t e = __ldg(&leafset[p]);
-          f = __dmul_rn(leaf_l[e & 0xffu], leaf_r[(e >> 8) & 0xffu]);
+          f = mul_rn_int(leaf_l[e & 0xffu], leaf_r[(e >> 8) & 0xffu]);
           set = (int)(e >> 16);
         } else if constexpr (MODE == kPointsProduct) {
           const uint64_t code = __ldg(&codes[p]);
@@ -117,10 +118,10 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
 #pragma unroll
           for (int k = 1; k < MAXD; ++k) {
             const double h = S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)];
-            if (k < m) L = __dmul_rn(L, h);
-            else if (k > m && k < d) R = __dmul_rn(R, h);
+            if (k < m) L = mul_rn_int(L, h);
+            else if (k > m && k < d) R = mul_rn_int(R, h);
           }
-          f = __dmul_rn(L, R);
+          f = mul_rn_int(L, R);
         } else {
           const uint64_t code = __ldg(&codes[p]);
           set = (int)(code >> 60);
@@ -130,7 +131,7 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
             x[k] = (k < d) ? S.tab[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)] : 0.0;
           f = fn.template eval<MAXD>(S.desc, x);
         }
-        if constexpr (SCALE) f = __dmul_rn(f, jac);
+        if constexpr (SCALE) f = mul_rn_int(f, jac);
         if (base == 0) S.fv[p] = f;
         const double* wr = &S.w[set * kWStride];
         const double2 w01 = *reinterpret_cast<const double2*>(wr);
@@ -231,7 +232,7 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
             const double* src = left ? srcl : srcr;
             const double* fk = left ? fl : fr;
             double* dst = left ? lb[k & 1] + i : rb[k & 1] + (i - nl);
-            *dst = __dmul_rn(src[e & 0xfffu], fk[e >> 12]);
+            *dst = mul_rn_int(src[e & 0xfffu], fk[e >> 12]);
           }
           off += nl + nr;
           __syncwarp();

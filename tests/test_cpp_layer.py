@@ -64,3 +64,18 @@ def test_workspace_functors_match_families(lib):
                  "xy_value", "nan3", "tabulated3", "regions5", "subregions5x5_peak2", "predict_split_peak2",
                  "predict_split_snapshot", "mcubes_gauss3", "quad_mcubes_gauss3", "mcubes_value"):
         assert case in names, case
+
+
+@pytest.mark.gpu
+def test_integer_pipe_multiply_matches_fp64_multiply():
+    """pg::mul_rn_int, the evaluation kernel's double multiply on the integer
+    pipe, equals __dmul_rn bit for bit on 2^30 products (random patterns,
+    exact products and ties, the whole exponent range with zeros and infinities)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "mul_check.cu")
+    exe = os.path.join(BUILD, "mul_check")
+    subprocess.check_call([_nvcc(), "-std=c++17", "-O3", "--fmad=false", "-gencode", "arch=compute_103a,code=sm_103a",
+                           src, "-o", exe])
+    p = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    print(p.stdout)
+    assert p.returncode == 0 and p.stdout.startswith("PASS"), p.stdout + p.stderr
