@@ -70,7 +70,8 @@ class PgStats(ctypes.Structure):
                 ("eval_ms", ctypes.c_double), ("stage_ms", ctypes.c_double), ("stage_bytes", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("tune_warps", ctypes.c_int32 * 2), ("tune_ctas_per_sm", ctypes.c_int32 * 2),
-                ("eval_bytes", ctypes.c_uint64), ("host_ms", ctypes.c_double), ("sync_ms", ctypes.c_double)]
+                ("eval_bytes", ctypes.c_uint64), ("host_ms", ctypes.c_double), ("sync_ms", ctypes.c_double),
+                ("spill_ms", ctypes.c_double), ("admit_ms", ctypes.c_double)]
 
 
 class PgMcubesOptions(ctypes.Structure):

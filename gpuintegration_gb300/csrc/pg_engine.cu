@@ -680,6 +680,10 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       }
       if (t > T) {
         if ((rc = grow_list(cur, t, maxd, T, P)) != PG_OK) return rc;
+        if (profiling) {
+          cudaEventRecord(ev_[8], stream_);
+          admit_timing_pending_ = true;
+        }
         if (!adm_pending.empty()) {
           const uint32_t m = (uint32_t)adm_pending.size();
           hs[m] = jobs[adm_pending.back()].start + jobs[adm_pending.back()].n;
@@ -728,6 +732,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
           J.sp = nullptr;
           J.sp_bytes = 0;
         }
+        if (profiling) cudaEventRecord(ev_[9], stream_);
         T = t;
         P = pp;
       }
@@ -836,7 +841,9 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       record(ev_[0], ev_[1], &stats.eval_ms);
       record(ev_[1], ev_[2], &stats.stage_ms);
       if (compact_timing_pending_) record(ev_[2 + 2], ev_[3 + 2], &stats.stage_ms);
-      compact_timing_pending_ = false;
+      if (spill_timing_pending_) record(ev_[6], ev_[7], &stats.spill_ms);
+      if (admit_timing_pending_) record(ev_[8], ev_[9], &stats.admit_ms);
+      compact_timing_pending_ = spill_timing_pending_ = admit_timing_pending_ = false;
     }
     const IterScalars* sc = (const IterScalars*)h_scal_.p;
     // Host decisions, per integral, exactly as Workspace::integrate.
@@ -966,6 +973,10 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     // separate pinned arrays that the host does not touch again before the
     // end-of-iteration synchronisation, so no copy here needs a host wait.
     Transition* hsp = (Transition*)h_trans_spill_.p;
+    if (!spill.empty() && profiling) {
+      cudaEventRecord(ev_[6], stream_);
+      spill_timing_pending_ = true;
+    }
     if (!spill.empty()) {
       std::memcpy(hsp, ht, njobs * sizeof(Transition));
       for (uint32_t j : spill) {
@@ -1011,6 +1022,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
              "transition upload");
       stats.h2d_bytes += njobs * sizeof(Transition);
+      if (profiling) cudaEventRecord(ev_[7], stream_);
     }
     const int nxt = cur ^ 1;
     if (out_total > 0) {
@@ -1041,7 +1053,9 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   }
   PG_TRY(cudaStreamSynchronize(stream_), "run");
   if (profiling && compact_timing_pending_) record(ev_[4], ev_[5], &stats.stage_ms);
-  compact_timing_pending_ = false;
+  if (profiling && spill_timing_pending_) record(ev_[6], ev_[7], &stats.spill_ms);
+  if (profiling && admit_timing_pending_) record(ev_[8], ev_[9], &stats.admit_ms);
+  compact_timing_pending_ = spill_timing_pending_ = admit_timing_pending_ = false;
   return PG_OK;
 }
 

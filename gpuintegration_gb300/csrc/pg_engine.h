@@ -241,7 +241,9 @@ class Engine {
   bool compact_timing_pending_ = false;
   // pinned host mirrors
   DevBuf h_segs_, h_chunks_, h_trans_, h_trans_spill_, h_scal_, h_live_, h_thr_, h_adm_starts_, h_adm_ids_;
-  cudaEvent_t ev_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // 0-1 evaluation, 1-2 stages, 4-5 compaction, 6-7 spills, 8-9 admission and restores
+  cudaEvent_t ev_[10] = {};
+  bool spill_timing_pending_ = false, admit_timing_pending_ = false;
 };
 
 }  // namespace pg

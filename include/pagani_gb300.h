@@ -130,6 +130,8 @@ typedef struct pg_stats {
   uint64_t eval_bytes;          /* algorithmic HBM bytes of the evaluation launches */
   double host_ms;               /* host time from an iteration's readback to the next evaluation launch */
   double sync_ms;               /* host time blocked waiting for an iteration's device work */
+  double spill_ms;              /* device time of moving region lists out of the pool (compaction + copies) */
+  double admit_ms;              /* device time of admissions: first splits and region lists moved back in */
 } pg_stats;
 
 void pg_options_default(pg_options* opt);
