@@ -269,6 +269,17 @@ def run_reference(args, cases, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(values, dist, device="cpu"):
+    """Element-wise maximum of `values` over the ranks of the process group (the
+    time of the slowest replica); the values themselves without a group."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
@@ -337,10 +348,7 @@ def main():
     ctx.set_profiling(False)
     dev_s = sum(dev_ms) / 1000.0
     wall_s = sum(wall)
-    if dist:
-        t = torch.tensor([dev_s, wall_s], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall_s = float(t[0]), float(t[1])
+    dev_s, wall_s = max_over_ranks([dev_s, wall_s], dist, f"cuda:{local}")
     converged = sum(conv_counts)
     value = world * converged / dev_s
     e2e = world * converged / wall_s
