@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cmath>
 #include <string>
 
@@ -24,6 +25,20 @@ constexpr int kCodesPerDim = 11;    // 0, +G0..+G4, -G0..-G4
 constexpr int kRedThreads = 256;
 constexpr int kRedItems = 8;
 constexpr int kChunk = kRedThreads * kRedItems;
+
+// Opts `kernel` into `bytes` of dynamic shared memory on the current device,
+// once per device (bit d of `done`); safe from several host threads.
+template <class Kernel>
+inline cudaError_t ensure_dynamic_smem(Kernel kernel, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_release);
+  return e;
+}
 
 // ---------------------------------------------------------------------------
 // Double-precision multiply on the integer pipe.  GB300 executes FP64 at 2

@@ -431,13 +431,9 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
 template <int MAXD, int WARPS, class Fn>
 inline cudaError_t launch_eval_shape(const pg_eval_args& a, const Fn& fn) {
   const size_t smem = sizeof(EvalWarpSmem<MAXD>) * WARPS;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(eval_kernel<MAXD, WARPS, Fn>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static std::atomic<unsigned long long> attr_done{0};
+  const cudaError_t ae = ensure_dynamic_smem(eval_kernel<MAXD, WARPS, Fn>, (int)smem, attr_done);
+  if (ae != cudaSuccess) return ae;
   const uint64_t want = (a.n + WARPS - 1) / WARPS;
   const uint64_t cap = (uint64_t)(a.num_sms > 0 ? a.num_sms : 1) * (uint64_t)(a.ctas_per_sm > 0 ? a.ctas_per_sm : 32);
   const uint64_t g = want < cap ? want : cap;

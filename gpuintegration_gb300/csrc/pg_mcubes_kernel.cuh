@@ -174,13 +174,9 @@ constexpr size_t kMcMaxSmem = 200 * 1024;
 // Host launch of one m-Cubes iteration for an integrand functor type Fn.
 template <int MAXD, class Fn>
 inline cudaError_t launch_mcubes(const pg_mcubes_args& a, const Fn& fn) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e =
-        cudaFuncSetAttribute(mcubes_kernel<MAXD, Fn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcMaxSmem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static std::atomic<unsigned long long> attr_done{0};
+  const cudaError_t ae = ensure_dynamic_smem(mcubes_kernel<MAXD, Fn>, (int)kMcMaxSmem, attr_done);
+  if (ae != cudaSuccess) return ae;
   mcubes_kernel<MAXD, Fn><<<kMcBlocks, kMcThreads, (size_t)a.smem, (cudaStream_t)a.stream>>>(
       *static_cast<const McArgs*>(a.args), fn);
   return cudaGetLastError();
