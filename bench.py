@@ -126,7 +126,7 @@ def ops_per_point(family, d):
     per evaluation point of the library's algorithm."""
     import gpuintegration_gb300 as pg
     if family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT):
-        f = 1 if d <= 8 else d - 1  # L * R from the half tries (d <= 8) or the pointwise two-half product
+        f = 1  # L * R from the half tries
     elif family == pg.OSCILLATORY:
         f = d + 1
     elif family == pg.CORNER_PEAK:
@@ -145,8 +145,7 @@ def ops_per_region(family, d):
     sep = family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT)
     factor = {pg.PRODUCT_PEAK: 3, pg.GAUSSIAN: 4, pg.C0: 3, pg.DISCONTINUOUS: 2, pg.PRODUCT: 0}.get(family, 0)
     m = d // 2  # half tries: depths 2..m of the left half, 2..d-m of the right half
-    trie = (sum(_feval(k) for k in range(2, m + 1)) + sum(_feval(k) for k in range(2, d - m + 1))) \
-        if (sep and d <= 8) else 0
+    trie = (sum(_feval(k) for k in range(2, m + 1)) + sum(_feval(k) for k in range(2, d - m + 1))) if sep else 0
     return 11 * d * (2 + factor) + trie + 320 + (5 * d + 2) + 113 + d
 
 

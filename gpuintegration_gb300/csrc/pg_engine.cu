@@ -296,7 +296,7 @@ int Engine::init(std::string* why) {
   code_coefficients(r2, R.A, R.B);
   std::vector<uint16_t> tries;
   std::vector<uint32_t> leafset;
-  for (int d = PG_MIN_NDIM; d <= kTrieMaxDim; ++d) {
+  for (int d = PG_MIN_NDIM; d <= kMaxNdim; ++d) {
     RuleTable t = make_rule(d);
     std::vector<uint16_t> inner;
     std::vector<uint32_t> leaf;

@@ -20,9 +20,8 @@ namespace pg {
 struct RuleDev {
   const uint64_t* code;             // packed points, concatenated over ndim
   const uint16_t* trie;             // inner entries of the half tries (split_trie in pg_rule.h),
-  int32_t trie_off[kMaxNdim + 1];   // concatenated over ndim <= kTrieMaxDim
-  // Per point of the ndim <= kTrieMaxDim rules: left node | right node << 8 |
-  // generator set << 16.
+  int32_t trie_off[kMaxNdim + 1];   // concatenated over ndim
+  // Per point of every rule: left node | right node << 12 | generator set << 24.
   const uint32_t* leafset;
   int32_t leafset_off[kMaxNdim + 1];
   const double* w;                  // [(kMaxNdim + 1) * 45]
@@ -45,27 +44,30 @@ struct RuleDev {
 // tree per 32-lane half, then (half0 + 0) + half1.  Each per-axis coordinate
 // value a region can take (centre, +-G0..G4) is computed once per region.
 // ---------------------------------------------------------------------------
-// Half-trie buffers of the d <= 8 kernel: per half, the depth-2 and depth-4
-// nodes (at most feval(4) = 153) share one buffer and the depth-3 nodes (at
-// most feval(3) = 77) use the other.  The area also holds the reduction trees
-// (325 doubles).
-constexpr int kTrieMaxDim = 8;
+// Half-trie buffers: per half, the nodes of even depths (2, 4, 6) share one
+// buffer and those of odd depths (3, 5) the other.  A half has at most 4 axes
+// in the d <= 8 kernel (depth-4 nodes: feval(4) = 153, depth 3: 77) and at
+// most 6 in the d <= 12 kernel (feval(6) = 453, feval(5) = 273).  The area
+// also holds the reduction trees (325 doubles).
 constexpr int kWStride = 6;  // padded row of the 5 rule weights of a generator set
-constexpr int kHalfEven = 160, kHalfOdd = 80;
-constexpr int kTrieBuf = 2 * (kHalfEven + kHalfOdd);
+
+template <int MAXD>
+struct HalfTrie {
+  static constexpr int even = MAXD <= 8 ? 160 : 456;
+  static constexpr int odd = MAXD <= 8 ? 80 : 280;
+  static constexpr int total = 2 * (even + odd);
+};
 
 template <int MAXD>
 struct EvalTrieSmem {
-  double a[kTrieBuf];  // left even | left odd | right even | right odd
+  double a[HalfTrie<MAXD>::total];  // left even | left odd | right even | right odd
 };
-template <>
-struct EvalTrieSmem<16> {};
 
 template <int MAXD>
 struct EvalWarpSmem {
   EvalTrieSmem<MAXD> trie;
   IntegralDesc desc;
-  double tab[MAXD * kCodesPerDim];  // (tab and fac double as the reduction area of the d > 8 kernel)
+  double tab[MAXD * kCodesPerDim];
   double fac[MAXD * kCodesPerDim];  // per-axis factors of separable integrands
   double fv[64];
   double lo[MAXD];
@@ -82,10 +84,9 @@ struct RuleSums {
 };
 
 // How a point's value is formed: from the half tries of per-axis factors
-// (product-form integrands, d <= 8: one multiply L * R), as the two-half
-// product of per-axis factors (product-form, d > 8), or by evaluating the
+// (product-form integrands: one multiply L * R), or by evaluating the
 // integrand on the point's coordinates.
-constexpr int kPointsTrie = 0, kPointsProduct = 1, kPointsEval = 2;
+constexpr int kPointsTrie = 0, kPointsEval = 2;
 
 // The per-point loop of eval_kernel: lane l takes points l, l+64, ... into a*
 // and l+32, l+96, ... into b*, in ascending order, with fused multiply-adds,
@@ -106,22 +107,8 @@ __device__ __forceinline__ void point_sums(RuleSums& rs, EvalWarpSmem<MAXD>& S, 
         int set;
         if constexpr (MODE == kPointsTrie) {
           const uint32_t e = __ldg(&leafset[p]);
-          f = mul_rn_int(leaf_l[e & 0xffu], leaf_r[(e >> 8) & 0xffu]);
-          set = (int)(e >> 16);
-        } else if constexpr (MODE == kPointsProduct) {
-          const uint64_t code = __ldg(&codes[p]);
-          set = (int)(code >> 60);
-          // L * R (m = d / 2), each half in axis order
-          const int m = d / 2;
-          double L = S.fac[(int)(code & 15u)];
-          double R = S.fac[m * kCodesPerDim + (int)((code >> (4 * m)) & 15u)];
-#pragma unroll
-          for (int k = 1; k < MAXD; ++k) {
-            const double h = S.fac[k * kCodesPerDim + (int)((code >> (4 * k)) & 15u)];
-            if (k < m) L = mul_rn_int(L, h);
-            else if (k > m && k < d) R = mul_rn_int(R, h);
-          }
-          f = mul_rn_int(L, R);
+          f = mul_rn_int(leaf_l[e & 0xfffu], leaf_r[(e >> 12) & 0xfffu]);
+          set = (int)(e >> 24);
         } else {
           const uint64_t code = __ldg(&codes[p]);
           set = (int)(code >> 60);
@@ -206,24 +193,27 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     if (sep)
       for (int v = lane; v < d * kCodesPerDim; v += 32) S.fac[v] = fn.factor(S.desc, v / kCodesPerDim, S.tab[v]);
     __syncwarp();
-    // Product-form integrands with d <= 8: the half products L (axes 0..m-1)
-    // and R (axes m..d-1), depth by depth, both halves' nodes of a depth in
-    // the same warp instructions (depth 1 is the factor row of the half's
-    // first axis).  Each point then takes one multiply, L * R.
+    // Product-form integrands: the half products L (axes 0..m-1) and R (axes
+    // m..d-1), depth by depth, both halves' nodes of a depth in the same warp
+    // instructions (depth 1 is the factor row of the half's first axis).  Each
+    // point then takes one multiply, L * R.
     const double* leaf_l = S.fac;
     const double* leaf_r = S.fac;
     const uint32_t* leafset = nullptr;
-    if constexpr (MAXD <= kTrieMaxDim) {
+    {
       if (sep) {
+        constexpr int ev = HalfTrie<MAXD>::even, od = HalfTrie<MAXD>::odd;
         const uint16_t* tt = rule.trie + rule.trie_off[d];
         const int m = d / 2, mr = d - m;
-        double* const lb[2] = {S.trie.a, S.trie.a + kHalfEven};
-        double* const rb[2] = {S.trie.a + kHalfEven + kHalfOdd, S.trie.a + 2 * kHalfEven + kHalfOdd};
+        // depth k of the left half at trie.a + (k odd ? ev : 0), of the right
+        // half at trie.a + ev + od + (k odd ? ev : 0)
+        double* const ta = S.trie.a;
         int off = 0;
         for (int k = 2; k <= mr; ++k) {  // mr >= m
           const int nl = (k <= m) ? rule.feval[k] : 0, nr = rule.feval[k];
-          const double* srcl = (k == 2) ? S.fac : lb[(k - 1) & 1];
-          const double* srcr = (k == 2) ? S.fac + m * kCodesPerDim : rb[(k - 1) & 1];
+          const int cur = (k & 1) ? ev : 0, prev = (k & 1) ? 0 : ev;
+          const double* srcl = (k == 2) ? S.fac : ta + prev;
+          const double* srcr = (k == 2) ? S.fac + m * kCodesPerDim : ta + ev + od + prev;
           const double* fl = S.fac + (k - 1) * kCodesPerDim;
           const double* fr = S.fac + (m + k - 1) * kCodesPerDim;
           for (int i = lane; i < nl + nr; i += 32) {
@@ -231,14 +221,14 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
             const bool left = i < nl;
             const double* src = left ? srcl : srcr;
             const double* fk = left ? fl : fr;
-            double* dst = left ? lb[k & 1] + i : rb[k & 1] + (i - nl);
+            double* dst = left ? ta + cur + i : ta + ev + od + cur + (i - nl);
             *dst = mul_rn_int(src[e & 0xfffu], fk[e >> 12]);
           }
           off += nl + nr;
           __syncwarp();
         }
-        leaf_l = (m == 1) ? S.fac : lb[m & 1];
-        leaf_r = (mr == 1) ? S.fac + m * kCodesPerDim : rb[mr & 1];
+        leaf_l = (m == 1) ? S.fac : ta + ((m & 1) ? ev : 0);
+        leaf_r = (mr == 1) ? S.fac + m * kCodesPerDim : ta + ev + od + ((mr & 1) ? ev : 0);
         leafset = rule.leafset + rule.leafset_off[d];
       }
     }
@@ -247,19 +237,15 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     // per-point instruction is spent on either decision.
     const double jac = S.desc.jac;
     RuleSums rs{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const int mode = (sep && leafset) ? kPointsTrie : (sep ? kPointsProduct : kPointsEval);
+    const int mode = (sep && leafset) ? kPointsTrie : kPointsEval;
     if (jac != 1.0) {
       if (mode == kPointsTrie)
         point_sums<MAXD, kPointsTrie, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
-      else if (mode == kPointsProduct)
-        point_sums<MAXD, kPointsProduct, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
       else
         point_sums<MAXD, kPointsEval, true>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
     } else {
       if (mode == kPointsTrie)
         point_sums<MAXD, kPointsTrie, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
-      else if (mode == kPointsProduct)
-        point_sums<MAXD, kPointsProduct, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
       else
         point_sums<MAXD, kPointsEval, false>(rs, S, fn, codes, feval, d, lane, leafset, leaf_l, leaf_r, jac);
     }
@@ -268,11 +254,7 @@ static __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     // (half0 + 0) + half1.  The same additions in the same pairs are done here
     // level by level on shared memory, packing the 10 trees' additions of a
     // level into as few warp instructions as possible.
-    double* red;  // free by now: the trie buffer (d <= 8 kernel) or tab + fac (352 doubles)
-    if constexpr (MAXD <= kTrieMaxDim)
-      red = S.trie.a;
-    else
-      red = S.tab;
+    double* red = S.trie.a;  // free by now (at least 480 doubles; 325 used)
     __syncwarp();
     red[0 * 32 + lane] = rs.a0;
     red[1 * 32 + lane] = rs.a1;

@@ -94,13 +94,16 @@ __device__ __forceinline__ double family_factor(const IntegralDesc& D, int k, do
 // for PRODUCT).
 template <int MAXD>
 __device__ __forceinline__ double split_product(const IntegralDesc& D, const double* x, bool factors) {
-  const int d = D.d, m = product_split(d);
+  const int d = D.d, m = product_split(d);  // 1 <= m < d
   double L = factors ? family_factor(D, 0, x[0]) : x[0];
-  double R = factors ? family_factor(D, m, x[m]) : x[m];
+  double R = 0.0;
 #pragma unroll
-  for (int i = 1; i < MAXD; ++i) {
-    if (i < m) L = __dmul_rn(L, factors ? family_factor(D, i, x[i]) : x[i]);
-    else if (i > m && i < d) R = __dmul_rn(R, factors ? family_factor(D, i, x[i]) : x[i]);
+  for (int i = 1; i < MAXD; ++i) {  // static indices keep x in registers
+    if (i >= d) break;
+    const double h = factors ? family_factor(D, i, x[i]) : x[i];
+    if (i < m) L = __dmul_rn(L, h);
+    else if (i == m) R = h;
+    else R = __dmul_rn(R, h);
   }
   return __dmul_rn(L, R);
 }

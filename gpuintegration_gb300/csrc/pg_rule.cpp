@@ -238,7 +238,7 @@ void split_trie(const RuleTable& r, std::vector<uint16_t>* inner, std::vector<ui
   }
   leaf->resize(r.feval);
   for (int p = 0; p < r.feval; ++p)
-    (*leaf)[p] = (uint32_t)ln[p] | ((uint32_t)rn[p] << 8) | ((uint32_t)(r.code[p] >> 60) << 16);
+    (*leaf)[p] = (uint32_t)ln[p] | ((uint32_t)rn[p] << 12) | ((uint32_t)(r.code[p] >> 60) << 24);
 }
 
 void code_coefficients(const RuleTable& r, double* A, double* B) {

@@ -42,8 +42,8 @@ RuleTable make_rule(int ndim);
 // code i.  `inner` lists, for depth k = 2, 3, ...: the left half's depth-k
 // entries (while k <= m), then the right half's (while k <= d - m); entry =
 // parent index (12 bits) | code << 12.  `leaf` gives per point, in rule
-// order: left node index at depth m | right node index at depth d - m << 8 |
-// generator set << 16.  A half of k axes has feval_count(k) nodes at depth k
+// order: left node index at depth m | right node index at depth d - m << 12 |
+// generator set << 24.  A half of k axes has feval_count(k) nodes at depth k
 // (feval_count(1) = 11).
 void split_trie(const RuleTable& r, std::vector<uint16_t>* inner, std::vector<uint32_t>* leaf);
 
