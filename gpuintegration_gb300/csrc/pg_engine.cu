@@ -619,10 +619,11 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     J.iters = 0;
     J.done = false;
     J.state = JOB_PENDING;
-    J.sp = nullptr;
-    J.sp_bytes = 0;
+    J.sp_batch = -1;
+    J.sp_off = J.sp_poff = 0;
   }
   spill_.reset();
+  spill_batches_.clear();
   const auto t_start = std::chrono::steady_clock::now();
   // Host decision time: from the end of an iteration's readback to the next
   // evaluation launch (the device idles in between unless work is queued).
@@ -712,12 +713,13 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
         for (uint32_t j : restore) {
           Job& J = jobs[j];
           const int d = J.desc.d;
-          const double* sl = J.sp;
-          const double* sn = J.sp + J.n * d;
-          const double* sq = J.sp + 2 * J.n * d;
-          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, sl, J.n * 8, J.n * 8, d,
+          SpillBatch& B = spill_batches_[J.sp_batch];
+          const double* sl = B.p + J.sp_off;
+          const double* sn = B.p + (uint64_t)B.rows * B.stride + J.sp_off;
+          const double* sq = B.p + 2ull * B.rows * B.stride + J.sp_poff;
+          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, sl, B.stride * 8, J.n * 8, d,
                                    cudaMemcpyHostToDevice, stream_), "restore");
-          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, sn, J.n * 8, J.n * 8, d,
+          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, sn, B.stride * 8, J.n * 8, d,
                                    cudaMemcpyHostToDevice, stream_), "restore");
           PG_TRY(cudaMemcpyAsync((double*)parent_[cur].p + J.par_start, sq, (J.n / 2) * 8, cudaMemcpyHostToDevice,
                                  stream_), "restore");
@@ -726,11 +728,11 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
           stats.launches++;
           PG_TRY(cudaGetLastError(), "restore launch");
           stats.h2d_bytes += J.n * 16 * d + J.n * 4;
-          // The slice may be handed out again at once: its next writer is a
-          // copy queued behind these on the same stream.
-          spill_.release(J.sp, J.sp_bytes);
-          J.sp = nullptr;
-          J.sp_bytes = 0;
+          // When the batch's last integral is back, its slice may be handed out
+          // again at once: the next writer is a copy queued behind these on the
+          // same stream.
+          if (--B.live == 0) spill_.release(B.p, B.bytes);
+          J.sp_batch = -1;
         }
         if (profiling) cudaEventRecord(ev_[9], stream_);
         T = t;
@@ -966,63 +968,94 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       }
       ht[j] = Tr;
     }
-    // Spilled integrals: each one's children go to offset 0 of a transient
-    // device buffer (one compaction per integral) and from there to pinned
-    // host memory; then every spilled integral is excluded (mode 0) from the
-    // compaction of the resident list.  The two transition tables are
-    // separate pinned arrays that the host does not touch again before the
-    // end-of-iteration synchronisation, so no copy here needs a host wait.
+    // Spilled integrals, in groups of at most one pool's worth of regions:
+    // the children of a group go to a transient device buffer in one
+    // compaction (integral j at its own offset, rows `stride` apart) and from
+    // there in three copies to one pinned slice (a spill batch); every spilled
+    // integral is then excluded (mode 0) from the compaction of the resident
+    // list.  The two transition tables are separate pinned arrays that the
+    // host does not touch again before the end-of-iteration synchronisation,
+    // so no copy here needs a host wait.
     Transition* hsp = (Transition*)h_trans_spill_.p;
-    if (!spill.empty() && profiling) {
-      cudaEventRecord(ev_[6], stream_);
-      spill_timing_pending_ = true;
-    }
     if (!spill.empty()) {
+      if (profiling) {
+        cudaEventRecord(ev_[6], stream_);
+        spill_timing_pending_ = true;
+      }
+      // groups [gbeg[g], gbeg[g+1]) of the spill list, with their region and parent totals
+      std::vector<size_t> gbeg{0};
+      std::vector<uint64_t> gsst, gspt;
+      uint64_t sst = 0, spt = 0, max_sst = 0, max_spt = 0;
       std::memcpy(hsp, ht, njobs * sizeof(Transition));
-      for (uint32_t j : spill) {
-        hsp[j].out_start = 0;
-        hsp[j].par_out = 0;
+      for (uint32_t j = 0; j < njobs; ++j) hsp[j].mode = 0;
+      for (size_t q = 0; q < spill.size(); ++q) {
+        const uint32_t j = spill[q];
+        const uint64_t n2 = 2 * keepA[j];
+        if (sst > 0 && sst + n2 > cap) {  // close the group
+          gsst.push_back(sst);
+          gspt.push_back(spt);
+          gbeg.push_back(q);
+          sst = spt = 0;
+        }
+        hsp[j] = ht[j];
+        hsp[j].out_start = sst;
+        hsp[j].par_out = spt;
+        jobs[j].sp_off = sst;
+        jobs[j].sp_poff = spt;
+        sst += n2;
+        spt += keepA[j];
+        max_sst = std::max(max_sst, sst);
+        max_spt = std::max(max_spt, spt);
         ht[j].mode = 0;
       }
+      gsst.push_back(sst);
+      gspt.push_back(spt);
+      gbeg.push_back(spill.size());
+      if ((rc = ensure(sp_left_, max_sst * maxd * 8)) != PG_OK) return rc;
+      if ((rc = ensure(sp_len_, max_sst * maxd * 8)) != PG_OK) return rc;
+      if ((rc = ensure(sp_par_, max_spt * 8)) != PG_OK) return rc;
       PG_TRY(cudaMemcpyAsync(trans_.p, hsp, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
              "transition upload");
       stats.h2d_bytes += njobs * sizeof(Transition);
-    } else {
-      PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
-             "transition upload");
-      stats.h2d_bytes += njobs * sizeof(Transition);
-    }
-    for (uint32_t j : spill) {
-      Job& J = jobs[j];
-      const SegDesc& S = hs[j];
-      const uint64_t A = keepA[j], n2 = 2 * A;
-      const int d = J.desc.d;
-      if ((rc = ensure(sp_left_, n2 * maxd * 8)) != PG_OK) return rc;
-      if ((rc = ensure(sp_len_, n2 * maxd * 8)) != PG_OK) return rc;
-      if ((rc = ensure(sp_par_, A * 8)) != PG_OK) return rc;
-      if ((rc = compact(cur, cur ^ 1, S.chunk_start, S.nchunks, maxd, (double*)sp_left_.p, (double*)sp_len_.p, n2,
-                        nullptr, (double*)sp_par_.p)) != PG_OK)
-        return rc;
-      J.sp_bytes = (2 * n2 * d + A) * 8;
-      J.sp = (double*)spill_.alloc(J.sp_bytes);
-      if (!J.sp) {
-        last_error = "pinned host memory for a spilled region list";
-        return PG_OOM;
+      for (size_t g = 0; g + 1 < gbeg.size(); ++g) {
+        const uint32_t jf = spill[gbeg[g]], jl = spill[gbeg[g + 1] - 1];
+        const uint32_t c0 = hs[jf].chunk_start, c1 = hs[jl].chunk_start + hs[jl].nchunks;
+        const uint64_t st = gsst[g], pt = gspt[g];
+        if ((rc = compact(cur, cur ^ 1, c0, c1 - c0, maxd, (double*)sp_left_.p, (double*)sp_len_.p, st, nullptr,
+                          (double*)sp_par_.p)) != PG_OK)
+          return rc;
+        SpillBatch B;
+        B.bytes = (2 * st * (uint64_t)maxd + pt) * 8;
+        B.p = (double*)spill_.alloc(B.bytes);
+        B.rows = maxd;
+        B.stride = st;
+        B.live = (int)(gbeg[g + 1] - gbeg[g]);
+        if (!B.p) {
+          last_error = "pinned host memory for spilled region lists";
+          return PG_OOM;
+        }
+        PG_TRY(cudaMemcpyAsync(B.p, sp_left_.p, st * maxd * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+        PG_TRY(cudaMemcpyAsync(B.p + st * maxd, sp_len_.p, st * maxd * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+        PG_TRY(cudaMemcpyAsync(B.p + 2 * st * maxd, sp_par_.p, pt * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+        stats.d2h_bytes += st * maxd * 16 + pt * 8;
+        const int bidx = (int)spill_batches_.size();
+        spill_batches_.push_back(B);
+        for (size_t q = gbeg[g]; q < gbeg[g + 1]; ++q) {
+          Job& J = jobs[spill[q]];
+          J.sp_batch = bidx;
+          J.state = JOB_SPILLED;
+          J.n = 2 * keepA[spill[q]];
+          J.has_parent = 1;
+        }
       }
-      // The transient buffer's rows are n2 apart; the slice keeps them packed.
-      PG_TRY(cudaMemcpyAsync(J.sp, sp_left_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-      PG_TRY(cudaMemcpyAsync(J.sp + n2 * d, sp_len_.p, n2 * d * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-      PG_TRY(cudaMemcpyAsync(J.sp + 2 * n2 * d, sp_par_.p, A * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-      stats.d2h_bytes += n2 * d * 16 + A * 8;
-      J.state = JOB_SPILLED;
-      J.n = n2;
-      J.has_parent = 1;
-    }
-    if (!spill.empty()) {
       PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
              "transition upload");
       stats.h2d_bytes += njobs * sizeof(Transition);
       if (profiling) cudaEventRecord(ev_[7], stream_);
+    } else {
+      PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
+             "transition upload");
+      stats.h2d_bytes += njobs * sizeof(Transition);
     }
     const int nxt = cur ^ 1;
     if (out_total > 0) {

@@ -112,11 +112,12 @@ struct Job {
   int error = 0;
   int state = JOB_PENDING;
   double done_ms = 0.0;  // host time from the start of the run to the iteration that finished it
-  // Next region list of a job moved out of the device pool, in the engine's
-  // pinned spill arena: rows [dim][n] of left, then of length, then the n/2
-  // parent estimates.
-  double* sp = nullptr;
-  size_t sp_bytes = 0;
+  // Next region list of a job moved out of the device pool: its place in a
+  // spill batch (pinned slice holding the lists of every integral spilled in
+  // one iteration: left rows [row][stride], length rows, parent estimates).
+  int sp_batch = -1;
+  uint64_t sp_off = 0;   // first region of the job within each row
+  uint64_t sp_poff = 0;  // first parent estimate of the job
   // Caller-given initial region list (host, SoA [dim * init_n + i]); 0
   // regions: the uniform split (Workspace.cuh:379-387).
   const double* init_left = nullptr;
@@ -238,6 +239,16 @@ class Engine {
   // transient device copy of one job's next list on its way to host memory
   DevBuf sp_left_, sp_len_, sp_par_;
   SpillArena spill_;
+  // Spill batches of the current run: slice, its size, rows and row stride
+  // (regions) of its region block, and the number of integrals still in it.
+  struct SpillBatch {
+    double* p;
+    size_t bytes;
+    int rows;
+    uint64_t stride;
+    int live;
+  };
+  std::vector<SpillBatch> spill_batches_;
   bool compact_timing_pending_ = false;
   // pinned host mirrors
   DevBuf h_segs_, h_chunks_, h_trans_, h_trans_spill_, h_scal_, h_live_, h_thr_, h_adm_starts_, h_adm_ids_;
