@@ -35,6 +35,16 @@ def test_header_compiles():
     assert os.path.getsize(out) > 0
 
 
+def test_functor_shapes_compile():
+    """Functor shapes of the reference's callers (host-device, non-const, float
+    arguments, integral return, device pointers, template operators) compile."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "functor_shapes.cu")
+    out = os.path.join(BUILD, "functor_shapes.o")
+    subprocess.check_call([_nvcc()] + _flags() + ["-c", src, "-o", out])
+    assert os.path.getsize(out) > 0
+
+
 @pytest.mark.parametrize("reference_first", [0, 1])
 def test_header_with_reference_types_either_order(reference_first):
     """numint::integration_result and quad::Volume come from whichever header is
