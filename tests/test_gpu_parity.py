@@ -5,7 +5,9 @@ Bit-exact for the stages that are integer/byte work or IEEE-exact arithmetic
 evaluation of integrands built from + - * / alone).  For integrands that call
 exp/cos/pow, the device math library and glibc may differ in the last bit, so
 estimates are compared at 1e-12 relative and error estimates at 1e-12 of the
-region's absolute estimate scale (the null rules cancel).
+region's absolute estimate scale: the null rules are differences of nearly equal
+rule sums, so a last-bit difference of f can move a region's error estimate by
+far more than one ulp of the error itself.
 """
 import math
 
