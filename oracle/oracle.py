@@ -1,6 +1,6 @@
 """ctypes wrapper of the CPU oracle (oracle/pagani_oracle.cpp).
 
-TEST INFRASTRUCTURE ONLY: the checker for the GB300 library.  Only tests/,
+TEST INFRASTRUCTURE ONLY: the oracle the GB300 library is tested against.  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this.
 """
 import ctypes

@@ -1,6 +1,6 @@
 // PAGANI CPU oracle -- TEST INFRASTRUCTURE ONLY.
 //
-// This file is the checker for the GB300 library: a plain C++ restatement of the
+// This file is the oracle of the GB300 library: a plain C++ restatement of the
 // reference's PAGANI adaptive-cubature iteration.  Only tests/, the smoke check
 // and bench.py's CPU-baseline leg may load it.  The product path never calls it.
 //

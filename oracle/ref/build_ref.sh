@@ -1,5 +1,5 @@
 #!/bin/sh
-# Builds the reference-derived checkers from the reference sources where they
+# Builds the reference-derived test programs from the reference sources where they
 # lie.  Outputs go only into oracle/_ref/ (git-ignored).  Needs the reference
 # tree (REF, default /root/reference); without it this script does nothing.
 set -e
