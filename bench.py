@@ -4,18 +4,32 @@
 Workload (one step): the 4096 pre-screened mixed Genz integrals of the
 batched configuration -- dim ~ U{2..8}, family ~ U{6 Genz families}, seeded
 a_i/u_i scaled per family, epsrel log-uniform in [1e-7, 1e-4], FP64, unit
-cube -- integrated together by pg_batch_integrate (one device region pool,
-one evaluation launch per iteration over every live region).
+cube -- integrated together by one pg_batch_integrate call (one device region
+pool of 2^26 regions, one evaluation launch per kernel run per iteration).
+Region evaluation uses generator-set sums for the product-form families
+(PG_EVAL_SET_SUMS; `--eval-mode points` selects the reference's
+point-by-point order).
 
 Metric: converged integrals per second, where an integral counts when PAGANI
 reports status 0 and the estimate lies within its epsrel of the analytic
-value.  `value` is timed with CUDA events on the library's stream (the step's
-integrand descriptors are a few MB; everything else is produced on the
-device); `e2e` is the same metric by host wall clock around the C-ABI call,
-including the host->device copy of the descriptors and the device->host copy
-of the results.  p50/p99 are the per-integral completion latencies inside a
-step.  The reference arm (--impl reference) times the CPU restatement of
-PAGANI on all host cores on a bounded sample of the same workload.
+value.  `value` is timed with CUDA events on the library's stream around each
+step (inputs already on the host side are a few MB of descriptors; the region
+pool lives on the device); `e2e` is the same metric by host wall clock around
+the C-ABI call, including the descriptor upload, the result download and the
+pinned-host traffic of region lists that leave the pool.  p50/p99 are the
+per-integral completion latencies inside a step.  After the timed steps the
+plain per-call path runs the same integrals one pg_integrate call at a time
+(the batched-over-plain ratio), and the CPU oracle runs a bounded sample; a
+wall-time budget bounds both legs so the whole run ends in time.
+
+The reference arm (--impl reference) times the CPU restatement of the
+reference's PAGANI iteration (oracle/, point by point, every host thread) on a
+fixed bounded sample of the workload per step, and reports its throughput
+extrapolated to the whole workload by evaluation count.
+
+`--config eval` times one evaluation kernel on a synthetic region list (the
+target of the ncu captures under profiles/); `--config 3` m-Cubes; `--config
+5` the served workload.
 """
 import argparse
 import ctypes
@@ -34,10 +48,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "integrals/s at rel err <=1e-6, batched vs plain PAGANI on 1 GB300; p50/p99 latency"
-# DRAM traffic of an evaluation launch over its algorithmic bytes, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a batched launch.
-DRAM_OVER_ALGORITHMIC = 1828488704 / 1800148656
 WORKLOAD = "batched PAGANI: 4096 pre-screened mixed Genz integrals, dim 2..8, 6 families, epsrel log-U[1e-7,1e-4]"
+SCREEN = os.path.join(ROOT, "tests", "golden", "config4_screen.json")
+EVAL_MODES = {"points": 0, "sets": 1}
+# DRAM bytes (read + write) of one evaluation launch over its algorithmic bytes
+# (16 d bytes of bounds in, 20 bytes of results out per region), from the ncu
+# capture of setsum_kernel on 1,048,576 8-D C0 regions: 145,437,952 bytes
+# against 134,217,728 + 20,971,520.
+DRAM_OVER_ALGORITHMIC = 145437952 / (134217728 + 20971520)
 
 
 def parse():
@@ -47,115 +65,28 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--count", type=int, default=4096)
-    p.add_argument("--plain-sample", type=int, default=256)
+    p.add_argument("--eval-mode", default="sets", choices=sorted(EVAL_MODES))
     p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--time-budget", type=float, default=1500.0,
+                   help="seconds the whole run may take; legs after the timed steps shrink or are skipped to fit")
     p.add_argument("--max-regions", type=int, default=1 << 26)
-    p.add_argument("--config", type=int, default=4, choices=[3, 4, 5],
+    p.add_argument("--config", default="4", choices=["3", "4", "5", "eval"],
                    help="4: batched workload (default, the metric's configuration); 5: served workload; "
-                        "3: m-Cubes Gaussian")
+                        "3: m-Cubes Gaussian; eval: one evaluation kernel on a synthetic region list")
     p.add_argument("--rate", type=float, default=2000.0, help="config 5: Poisson arrival rate (requests/s)")
     p.add_argument("--duration", type=float, default=60.0, help="config 5: arrival window (s)")
     p.add_argument("--budget-gb", type=float, default=120.0, help="config 5: device budget of the region pool")
     p.add_argument("--serve-seconds", type=float, default=0.0,
                    help="config 5: stop serving after this many seconds (0: arrival window + 60 s)")
+    p.add_argument("--family", default="c0", help="config eval: integrand family name")
+    p.add_argument("--ndim", type=int, default=8, help="config eval: dimension")
+    p.add_argument("--regions", type=int, default=1 << 20, help="config eval: regions per launch")
     return p.parse_args()
-
-
-def run_served(args):
-    """Served PAGANI (Poisson arrivals, continuous batching, HBM budget)."""
-    import gpuintegration_gb300 as pg
-    from gpuintegration_gb300 import workloads as W
-    arrivals = W.poisson_arrivals(args.rate, args.duration)
-    cases = W.config5_cases(len(arrivals))
-    ctx = pg.Context(0)
-    fs = (pg.PgIntegrand * len(cases))(*[c.integrand.to_c() for c in cases])
-    eps = np.array([c.epsrel for c in cases])
-    clocks = ClockSampler(0)
-    clocks.start()
-    deadline = 1000.0 * (args.serve_seconds if args.serve_seconds > 0 else args.duration + 60.0)
-    t0 = time.perf_counter()
-    res, done = ctx.serve(fs, eps, 0.0, arrivals, budget_bytes=int(args.budget_gb * 1e9), deadline_ms=deadline)
-    wall = time.perf_counter() - t0
-    clk = clocks.stop()
-    fin = done >= 0
-    lat = (done - arrivals)[fin]
-    arrived = int((arrivals <= wall * 1000.0).sum())
-    conv = sum(1 for c, r, ok in zip(cases, res, fin) if ok and within(c, r))
-    st = ctx.stats()
-    line = {"metric": "served PAGANI: integrals/s and p50/p99 latency", "value": conv / wall, "unit": "integrals/s",
-            "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"Poisson arrivals {args.rate:g}/s for {args.duration:g} s, Genz dim 3..10, "
-                                   f"epsrel log-U[1e-6,1e-3]", "requests": len(cases), "budget_gb": args.budget_gb,
-                       "deadline_s": deadline / 1000.0},
-            "latency_ms_finished": {"p50": float(np.percentile(lat, 50)) if lat.size else None,
-                                    "p99": float(np.percentile(lat, 99)) if lat.size else None,
-                                    "max": float(lat.max()) if lat.size else None},
-            "arrived": arrived, "finished": int(fin.sum()), "unfinished_at_deadline": int((~fin).sum()),
-            "wall_s": wall, "converged_within_tolerance": conv,
-            "status0": sum(1 for r, ok in zip(res, fin) if ok and r.status == 0),
-            "gpu_launches": int(st.launches), "points_per_s": st.points_evaluated / wall, "clocks": clk}
-    print(json.dumps(line), flush=True)
-
-
-def run_mcubes(args):
-    """m-Cubes on the 6-D sigma = 0.01 Gaussian (2^24 calls x 20 iterations, fixed seed)."""
-    import gpuintegration_gb300 as pg
-    from gpuintegration_gb300 import workloads as W
-    ctx = pg.Context(0)
-    f = W.config3_integrand()
-    for _ in range(args.warmup):
-        ctx.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 24, titer=20, itmax=20, skip=5, seed=2024)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r = ctx.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 24, titer=20, itmax=20, skip=5, seed=2024)
-    el = (time.perf_counter() - t0) / args.steps
-    line = {"metric": "m-Cubes time to solution, 6-D Gaussian sigma 0.01", "value": el * 1000, "unit": "ms",
-            "higher_is_better": False, "dtype": "f64", "data": "synthetic",
-            "estimate": r.estimate, "errorest": r.errorest, "sigma_from_1": (r.estimate - 1.0) / r.errorest,
-            "iters": r.iters, "status": r.status, "samples_per_s": r.neval / el}
-    print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------
 def _feval(d):
     return 1 + 8 * d + 2 * d * (d - 1) + 4 * d * (d - 1) + 4 * d * (d - 1) * (d - 2) // 3 + (1 << d)
-
-
-def ops_per_point(family, d):
-    """Algorithmic FP64 operations (add, mul, FMA, compare, one per libm call)
-    per evaluation point of the library's algorithm."""
-    import gpuintegration_gb300 as pg
-    if family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT):
-        f = 1  # L * R from the half tries
-    elif family == pg.OSCILLATORY:
-        f = d + 1
-    elif family == pg.CORNER_PEAK:
-        e, muls = d + 1, 0
-        while e:
-            muls += (e & 1) + (1 if e > 1 else 0)
-            e >>= 1
-        f = d + muls + 1
-    else:
-        f = d + 1
-    return f + 5  # five rule sums, one FMA each
-
-
-def ops_per_region(family, d):
-    import gpuintegration_gb300 as pg
-    sep = family in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT)
-    factor = {pg.PRODUCT_PEAK: 3, pg.GAUSSIAN: 4, pg.C0: 3, pg.DISCONTINUOUS: 2, pg.PRODUCT: 0}.get(family, 0)
-    m = d // 2  # half tries: depths 2..m of the left half, 2..d-m of the right half
-    trie = (sum(_feval(k) for k in range(2, m + 1)) + sum(_feval(k) for k in range(2, d - m + 1))) if sep else 0
-    return 11 * d * (2 + factor) + trie + 320 + (5 * d + 2) + 113 + d
-
-
-def algorithmic_ops(cases, results):
-    tot = 0.0
-    for c, r in zip(cases, results):
-        f = c.integrand
-        regions = r.neval // _feval(f.ndim)
-        tot += r.neval * ops_per_point(f.family, f.ndim) + regions * ops_per_region(f.family, f.ndim)
-    return tot
 
 
 class ClockSampler:
@@ -208,63 +139,237 @@ def within(c, r):
     return r.status == 0 and W.within_tolerance(r.estimate, c.exact, c.epsrel)
 
 
+def load_screen():
+    return json.load(open(SCREEN))
+
+
+# ---------------------------------------------------------------------------
+# Roofline of region evaluation.  The kernels are bound by the FP64 pipe
+# (GB300: 2 FP64 lanes per SM per clock, one pipe slot per FP64 instruction
+# whether FMA, multiply or add), so their work is counted in FP64 operations
+# per region of each kernel's algorithm, and the peak is this GPU's FP64
+# instruction rate, measured by pg_probe_fp64_peak (an FMA loop; TFLOP/s / 2).
+# The driver's peak file holds HBM and bf16 figures only.  A libm call or a
+# division counts the FP64 instructions it executes on this GPU, measured by
+# ncu (smsp__sass_thread_inst_executed_op_fp64_pred_on per region, less the
+# counted arithmetic: profiles/setsum_kernel_fp64_mix.md).  Multiplies the
+# kernels run on the integer pipe (pg::mul_rn_int) are not FP64 operations.
+LIBM_OPS = {"exp": 17.2, "div": 6.2, "cos": 22.0}
+
+
+def _factor_ops(family):
+    import gpuintegration_gb300 as pg
+    return {pg.PRODUCT_PEAK: 2 + LIBM_OPS["div"],    # sub, fma, 1/()
+            pg.GAUSSIAN: 4 + LIBM_OPS["exp"],        # sub, mul, mul, normalisation test, exp
+            pg.C0: 2 + LIBM_OPS["exp"],              # sub, mul, exp
+            pg.DISCONTINUOUS: 2 + LIBM_OPS["exp"],   # compare, mul, exp
+            pg.PRODUCT: 0}.get(family, 0)
+
+
+def setsum_ops(family, d, unit=True):
+    """FP64 operations of one region of setsum_kernel (PG_EVAL_SET_SUMS): per axis 11
+    coordinates (1 FMA, 2 off the unit cube), 11 factors, 5 pair sums, 8 recurrence FMAs;
+    per region 40 rule-sum FMAs, the fourth differences (5 d + 1) and 27 null-rule FMAs plus 6."""
+    axis = 11 * (1 if unit else 2) + 11 * _factor_ops(family) + 5 + 8
+    return d * axis + 40 + (5 * d + 1) + 27 + 6
+
+
+def points_ops(family, d, unit=True):
+    """FP64 operations of one region of eval_kernel (PG_EVAL_POINTS): 5 rule-sum FMAs per point,
+    the pointwise integrand of the non-product families, the per-axis factors of the product
+    families, and the per-region reduction trees (320 adds), null rules and tail."""
+    import gpuintegration_gb300 as pg
+    fe = _feval(d)
+    per_point = 5
+    if family == pg.OSCILLATORY:
+        per_point += d + LIBM_OPS["cos"]
+    elif family == pg.CORNER_PEAK:
+        per_point += d + LIBM_OPS["div"] + 4
+    return fe * per_point + 11 * d * ((1 if unit else 2) + _factor_ops(family)) + 320 + 27 + 6 * d
+
+
+# ---------------------------------------------------------------------------
+def run_served(args):
+    """Served PAGANI (Poisson arrivals, continuous batching, HBM budget)."""
+    import gpuintegration_gb300 as pg
+    from gpuintegration_gb300 import workloads as W
+    arrivals = W.poisson_arrivals(args.rate, args.duration)
+    cases = W.config5_cases(len(arrivals))
+    ctx = pg.Context(0)
+    fs = (pg.PgIntegrand * len(cases))(*[c.integrand.to_c() for c in cases])
+    eps = np.array([c.epsrel for c in cases])
+    opt = pg.default_options(eval_mode=EVAL_MODES[args.eval_mode])
+    clocks = ClockSampler(0)
+    clocks.start()
+    deadline = 1000.0 * (args.serve_seconds if args.serve_seconds > 0 else args.duration + 60.0)
+    t0 = time.perf_counter()
+    res, done = ctx.serve(fs, eps, 0.0, arrivals, budget_bytes=int(args.budget_gb * 1e9), deadline_ms=deadline,
+                          options=opt)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    fin = done >= 0
+    lat = (done - arrivals)[fin]
+    arrived = int((arrivals <= wall * 1000.0).sum())
+    conv = sum(1 for c, r, ok in zip(cases, res, fin) if ok and within(c, r))
+    st = ctx.stats()
+    line = {"metric": "served PAGANI: integrals/s and p50/p99 latency", "value": conv / wall, "unit": "integrals/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"Poisson arrivals {args.rate:g}/s for {args.duration:g} s, Genz dim 3..10, "
+                                   f"epsrel log-U[1e-6,1e-3]", "requests": len(cases), "budget_gb": args.budget_gb,
+                       "deadline_s": deadline / 1000.0, "eval_mode": args.eval_mode},
+            "latency_ms_finished": {"p50": float(np.percentile(lat, 50)) if lat.size else None,
+                                    "p99": float(np.percentile(lat, 99)) if lat.size else None,
+                                    "max": float(lat.max()) if lat.size else None},
+            "arrived": arrived, "finished": int(fin.sum()), "unfinished_at_deadline": int((~fin).sum()),
+            "wall_s": wall, "converged_within_tolerance": conv,
+            "status0": sum(1 for r, ok in zip(res, fin) if ok and r.status == 0),
+            "gpu_launches": int(st.launches), "points_per_s": st.points_evaluated / wall, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_mcubes(args):
+    """m-Cubes on the 6-D sigma = 0.01 Gaussian (2^24 calls x 20 iterations, fixed seed)."""
+    import gpuintegration_gb300 as pg
+    from gpuintegration_gb300 import workloads as W
+    ctx = pg.Context(0)
+    f = W.config3_integrand()
+    for _ in range(args.warmup):
+        ctx.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 24, titer=20, itmax=20, skip=5, seed=2024)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = ctx.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 24, titer=20, itmax=20, skip=5, seed=2024)
+    el = (time.perf_counter() - t0) / args.steps
+    line = {"metric": "m-Cubes time to solution, 6-D Gaussian sigma 0.01", "value": el * 1000, "unit": "ms",
+            "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "estimate": r.estimate, "errorest": r.errorest, "sigma_from_1": (r.estimate - 1.0) / r.errorest,
+            "iters": r.iters, "status": r.status, "samples_per_s": r.neval / el}
+    print(json.dumps(line), flush=True)
+
+
+def run_eval(args):
+    """One evaluation kernel on a synthetic list of dyadic regions (device buffers), CUDA-event timed."""
+    import torch
+    import gpuintegration_gb300 as pg
+    fam = {v: k for k, v in pg.FAMILY_NAMES.items()}[args.family]
+    d, n, mode = args.ndim, args.regions, EVAL_MODES[args.eval_mode]
+    ctx = pg.Context(0)
+    rng = np.random.default_rng(1)
+    a = rng.random(d)
+    a *= 12.0 / a.sum()
+    f = pg.Integrand(fam, d, list(a), list(rng.random(d)))
+    depth = rng.integers(0, 8, size=(d, n))
+    length = 0.5 ** depth
+    left = np.floor(rng.random((d, n)) / length) * length
+    dev = torch.device("cuda:0")
+    L, N = torch.from_numpy(left).to(dev), torch.from_numpy(length).to(dev)
+    est = torch.empty(n, dtype=torch.float64, device=dev)
+    err = torch.empty_like(est)
+    bis = torch.empty(n, dtype=torch.int32, device=dev)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
+    fc = f.to_c()
+
+    def launch():
+        rc = ctx.lib.pg_evaluate_regions_device(ctx.h, ctypes.byref(fc), None, None, n, L.data_ptr(), N.data_ptr(),
+                                                est.data_ptr(), err.data_ptr(), bis.data_ptr(), mode)
+        if rc != 0:
+            raise RuntimeError(ctx.lib.pg_last_error(ctx.h).decode())
+
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ops = (setsum_ops if mode == 1 and fam in (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT)
+           else points_ops)(fam, d) * n
+    peak = ctx.probe_fp64_peak() / 2.0
+    achieved = ops / (ms / 1000.0) / 1e12
+    line = {"metric": "region evaluations/s", "value": n / (ms / 1000.0), "unit": "regions/s", "ms_per_launch": ms,
+            "config": {"workload": f"{args.family} d={d}, {n} dyadic regions", "eval_mode": args.eval_mode},
+            "rule_points_per_s": n * _feval(d) / (ms / 1000.0),
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "T FP64 ops/s",
+                         "frac": achieved / peak, "fp64_ops_per_region": ops / n,
+                         "peak_source": "pg_probe_fp64_peak (FP64 FMA instruction rate of this GPU)"}}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------------
 CPU_SAMPLE_MAX_REGIONS = 200000
 
 
-def cpu_leg(cases, seconds, totals=None):
-    """Times the CPU oracle (all host threads) on the integrals of the workload,
-    in workload order, whose screened region count is at most
-    CPU_SAMPLE_MAX_REGIONS (so no single integral runs for minutes), until
-    `seconds` have passed; returns evaluation points/s and the sample."""
-    from oracle import oracle
-    oracle.load()
-    screen = json.load(open(os.path.join(ROOT, "tests", "golden", "config4_screen.json")))
-    threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    pts, done, conv = 0, 0, 0
-    for c, nreg in zip(cases, screen["nregions"]):
+def cpu_sample(cases, screen, point_budget, seed=4242):
+    """A fixed sample of the workload for the CPU oracle: integrals in a seeded
+    random order, skipping any whose screened region count exceeds
+    CPU_SAMPLE_MAX_REGIONS, until their evaluation count reaches point_budget."""
+    order = np.random.default_rng(seed).permutation(len(cases))
+    out, pts = [], 0
+    for i in order:
+        nreg = screen["nregions"][i]
         if nreg > CPU_SAMPLE_MAX_REGIONS:
             continue
+        ne = screen["neval"][i]
+        if pts + ne > point_budget and out:
+            continue
+        out.append(int(i))
+        pts += ne
+        if pts >= point_budget:
+            break
+    return out
+
+
+def cpu_leg(cases, idx):
+    """Runs the CPU oracle (point by point, every host thread) over cases[idx];
+    returns evaluation points/s and the sample's size and time."""
+    from oracle import oracle
+    oracle.load()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    pts, conv = 0, 0
+    for i in idx:
+        c = cases[i]
         r, _ = oracle.integrate(c.integrand, c.epsrel, 0.0, nthreads=threads)
         pts += r.neval
-        done += 1
         conv += 1 if within(c, r) else 0
-        if time.perf_counter() - t0 >= seconds:
-            break
     el = time.perf_counter() - t0
-    return {"points_per_s": pts / el, "integrals": done, "converged": conv, "seconds": el, "threads": threads}
+    return {"points_per_s": pts / el, "points": pts, "integrals": len(idx), "converged": conv, "seconds": el,
+            "threads": threads}
 
 
 def run_reference(args, cases, rank, world):
-    """Reference arm: the CPU restatement of PAGANI on every host core."""
+    """Reference arm: the CPU restatement of the reference's PAGANI on every host core, rank 0 only."""
     if rank != 0:
         return
-    total_pts = None
-    screen = json.load(open(os.path.join(ROOT, "tests", "golden", "config4_screen.json")))
-    import gpuintegration_gb300 as pg
-    lib = pg.load_library()
-    # evaluation count of the whole workload, from the screen run (leaf regions x points, x2 for inner nodes)
-    fe = [lib.pg_feval(c.integrand.ndim) for c in cases]
-    total_pts = float(sum(2 * n * f for n, f in zip(screen["nregions"][:len(cases)], fe)))
+    screen = load_screen()
+    total_pts = float(sum(screen["neval"][:len(cases)]))
+    # each step: the same fixed sample, a few seconds of CPU work on the GPU box's host
+    budget = max(1e8, 2e9 * args.cpu_seconds / 20.0)
+    idx = cpu_sample(cases, screen, budget)
     vals = []
     for i in range(args.warmup + args.steps):
-        s = cpu_leg(cases, args.cpu_seconds / 2)
+        s = cpu_leg(cases, idx)
         if i >= args.warmup:
             vals.append(s)
-    pps = sum(v["points_per_s"] for v in vals) / len(vals)
+    pps = sum(v["points"] for v in vals) / sum(v["seconds"] for v in vals)
     value = len(cases) / (total_pts / pps)
-    sample = f"first {vals[-1]['integrals']} integrals of the workload per step, extrapolated by evaluation count"
+    ms = 1000.0 * sum(v["seconds"] for v in vals) / len(vals)
+    sample = (f"each step: the same {len(idx)} integrals of the workload ({vals[-1]['points']:.3g} rule points, "
+              f"seeded random order, <= {CPU_SAMPLE_MAX_REGIONS} screened regions each); value = the workload's "
+              f"integral count / (its {total_pts:.3g} rule points / the sample's points per second)")
     line = {"metric": METRIC, "value": value, "unit": "integrals/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * vals[-1]["seconds"], "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "count": len(cases), "l2": "n/a (CPU)"},
+            "config": {"workload": WORKLOAD, "count": len(cases), "l2": "n/a (CPU)", "eval_mode": "points"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "integrals/s", "cores": vals[-1]["threads"], "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "integrals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "converged_in_sample": vals[-1]["converged"],
             "note": "no CPU PAGANI in the reference (Cuhre via cubacpp needs libcuba, absent); the oracle port "
-                    "restates the reference's CUDA iteration on host threads"}
+                    "restates the reference's CUDA iteration point by point on host threads"}
     print(json.dumps(line), flush=True)
 
 
@@ -280,23 +385,43 @@ def max_over_ranks(values, dist, device="cpu"):
 
 
 # ---------------------------------------------------------------------------
-def main():
-    args = parse()
-    if args.config == 5 and args.impl == "gb300":
-        return run_served(args)
-    if args.config == 3 and args.impl == "gb300":
-        return run_mcubes(args)
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    from gpuintegration_gb300 import workloads as W
-    cases = W.config4_cases(args.count)
-    if args.impl == "reference":
-        run_reference(args, cases, rank, world)
-        return
+def roofline(ctx, cases, results, st, steps, mode):
+    """Roofline of the dominant kernel (region evaluation, FP64 pipe)."""
+    import gpuintegration_gb300 as pg
+    sep = (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT)
+    ops = 0.0
+    for c, r in zip(cases, results):
+        f = c.integrand
+        regions = r.neval // _feval(f.ndim)
+        per = setsum_ops(f.family, f.ndim) if (mode == 1 and f.family in sep) else points_ops(f.family, f.ndim)
+        ops += regions * per
+    ops *= steps
+    eval_s = st.eval_ms / 1000.0
+    achieved = ops / eval_s / 1e12
+    peak = ctx.probe_fp64_peak() / 2.0
+    launches = max(st.eval_launches, 1)
+    alg_bytes = st.eval_bytes / launches
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "T FP64 ops/s", "frac": achieved / peak,
+            "traffic": alg_bytes * DRAM_OVER_ALGORITHMIC,
+            "kernel": "setsum_kernel" if mode == 1 else "eval_kernel",
+            "peak_source": "FP64 instruction rate of this GPU: pg_probe_fp64_peak's FMA loop (TFLOP/s / 2); "
+                           "MEASURED_PEAKS.json has HBM and bf16 figures only",
+            "fp64_ops_per_step": ops / steps,
+            "op_model": "FP64 operations per region of the kernel's algorithm (libm calls and divisions at their "
+                        "ncu-measured FP64 instruction counts); agrees with ncu's FP64 instruction count within "
+                        "a few per cent",
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "traffic_note": "algorithmic bytes x the DRAM/algorithmic ratio ncu measured on a 1M-region 8-D "
+                            "setsum_kernel launch",
+            "hbm_gbs_of_eval": st.eval_bytes / eval_s / 1e9}
 
+
+def run_batched(args, rank, world, local, t_begin):
     import torch
     import gpuintegration_gb300 as pg
+    from gpuintegration_gb300 import workloads as W
+    cases = W.config4_cases(args.count)
+    mode = EVAL_MODES[args.eval_mode]
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -307,7 +432,7 @@ def main():
     n = len(cases)
     fs = (pg.PgIntegrand * n)(*[c.integrand.to_c() for c in cases])
     eps = np.array([c.epsrel for c in cases])
-    opt = pg.default_options(max_regions=args.max_regions)
+    opt = pg.default_options(max_regions=args.max_regions, eval_mode=mode)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")  # > 129 MB L2
 
     def step(completion=None):
@@ -345,90 +470,102 @@ def main():
     dev_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
     st = ctx.stats()
     ctx.set_profiling(False)
-    dev_s = sum(dev_ms) / 1000.0
-    wall_s = sum(wall)
-    dev_s, wall_s = max_over_ranks([dev_s, wall_s], dist, f"cuda:{local}")
+    dev_s, wall_s = max_over_ranks([sum(dev_ms) / 1000.0, sum(wall)], dist, f"cuda:{local}")
     converged = sum(conv_counts)
     value = world * converged / dev_s
     e2e = world * converged / wall_s
     lat_all = np.concatenate(lat)
-    # Roofline of the dominant kernel (region evaluation, FP64 pipe), in FP64
-    # operations per second against the measured FP64 FMA instruction rate.
-    alg = algorithmic_ops(cases, results) * args.steps
-    achieved = alg / (st.eval_ms / 1000.0) / 1e12
-    peak = ctx.probe_fp64_peak() / 2.0
-    # DRAM bytes per evaluation launch: the launch's algorithmic bytes (region
-    # bounds in, estimate/error/split axis out, owner index) times the ratio
-    # ncu measured on one batched evaluation launch of this workload (14.27M
-    # regions of the first 4096 integrals, iteration 8: 1.830 GB read+written
-    # against 1.800 GB algorithmic).
-    alg_bytes_per_launch = st.eval_bytes / max(st.eval_launches, 1)
-    traffic = alg_bytes_per_launch * DRAM_OVER_ALGORITHMIC
-    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "FP64 Top/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "eval_kernel",
-            "peak_source": "measured FP64 FMA instruction rate of this GPU (pg_probe_fp64_peak, TFLOP/s / 2); "
-                           "MEASURED_PEAKS.json has no FP64 figure",
-            "algorithmic_ops_per_step": alg / args.steps,
-            "algorithmic_bytes_per_launch": alg_bytes_per_launch,
-            "eval_ms_per_step": st.eval_ms / args.steps, "stage_ms_per_step": st.stage_ms / args.steps,
-            "host_decision_ms_per_step": st.host_ms / args.steps,
-            "spill_ms_per_step": st.spill_ms / args.steps, "admit_ms_per_step": st.admit_ms / args.steps,
-            "note": "the point loop's multiplies run on the integer pipe (bit-identical to the FP64 multiply); "
-                    "achieved counts every algorithmic multiply as an FP64 operation",
-            "stage_gbs": (st.stage_bytes / max(st.stage_ms, 1e-9)) / 1e6,
-            "autotuned_launch": {"warps_per_block": list(st.tune_warps), "ctas_per_sm": list(st.tune_ctas_per_sm)}}
+    screen = load_screen()
     line = {"metric": METRIC, "value": value, "unit": "integrals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "count": n, "pool_regions": args.max_regions,
-                       "l2": "256 MB flush before every step", "seed": "config4_screen.json master 4096"},
+                       "l2": "256 MB flush before every step", "seed": "config4_screen.json master 4096",
+                       "eval_mode": args.eval_mode,
+                       "screen": f"{len(screen['accepted'])} of the first {screen['accepted'][-1] + 1} candidates "
+                                 f"converge within tolerance (unscreened pass rate "
+                                 f"{len(screen['accepted']) / (screen['accepted'][-1] + 1):.3f})"},
             "e2e": {"value": e2e, "unit": "integrals/s", "h2d_bytes_per_step": st.h2d_bytes // args.steps,
                     "d2h_bytes_per_step": st.d2h_bytes // args.steps},
-            "gpu_launches": int(st.launches), "clocks": clk, "roofline": roof,
+            "gpu_launches": int(st.launches), "clocks": clk,
+            "roofline": roofline(ctx, cases, results, st, args.steps, mode),
             "latency_ms": {"p50": float(np.percentile(lat_all, 50)), "p99": float(np.percentile(lat_all, 99))},
-            "converged_per_step": conv_counts, "points_per_s": st.points_evaluated / dev_s,
-            "regions_per_step": st.regions_evaluated // args.steps}
+            "converged_per_step": conv_counts, "rule_points_per_s": st.points_evaluated / dev_s,
+            "regions_per_step": st.regions_evaluated // args.steps,
+            "step_breakdown_ms": {"evaluation": st.eval_ms / args.steps, "stages": st.stage_ms / args.steps,
+                                  "host_decisions": st.host_ms / args.steps, "spill": st.spill_ms / args.steps,
+                                  "admission": st.admit_ms / args.steps},
+            "setsum_region_share": st.setsum_regions / max(st.regions_evaluated, 1)}
     if rank == 0:
-        # Plain per-call path on the same GPU, on a sample (batched on the same sample for the ratio).
-        ns = min(args.plain_sample, n)
-        sub = cases[:ns]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for c in sub:
-            ctx.integrate(c.integrand, c.epsrel, 0.0)
-        plain_s = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        ctx.batch_integrate([c.integrand for c in sub], [c.epsrel for c in sub], 0.0, options=opt)
-        batch_s = time.perf_counter() - t0
-        line["plain"] = {"sample": f"first {ns} integrals of the workload",
-                         "plain_integrals_per_s": ns / plain_s, "batched_integrals_per_s": ns / batch_s,
-                         "batched_over_plain": plain_s / batch_s}
-        # Where batching pays: the light integrals (<= 20000 regions when screened), whose plain
-        # runs are bound by per-iteration launches and synchronisation rather than by FP64 work.
-        screen = json.load(open(os.path.join(ROOT, "tests", "golden", "config4_screen.json")))
-        light = [c for c, nr in zip(cases, screen["nregions"]) if nr <= 20000][:1024]
-        t0 = time.perf_counter()
-        for c in light:
-            ctx.integrate(c.integrand, c.epsrel, 0.0)
-        pl = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        ctx.batch_integrate([c.integrand for c in light], [c.epsrel for c in light], 0.0, options=opt)
-        bl = time.perf_counter() - t0
-        line["plain_light"] = {"sample": f"first {len(light)} integrals with <= 20000 screened regions",
-                               "plain_integrals_per_s": len(light) / pl, "batched_integrals_per_s": len(light) / bl,
-                               "batched_over_plain": pl / bl}
+        step_s = wall_s / args.steps
+        left = args.time_budget - (time.perf_counter() - t_begin)
+        # Plain per-call path on the same GPU: every integral of the workload by
+        # its own pg_integrate call, when it fits the budget; else a seeded
+        # random sample, extrapolated to the workload by evaluation count.
+        popt = pg.default_options(eval_mode=mode)
+        tot_pts = float(sum(screen["neval"][:n]))
+        if left > 3.0 * step_s + args.cpu_seconds + 60.0:
+            t0 = time.perf_counter()
+            pres = [ctx.integrate(c.integrand, c.epsrel, 0.0, options=popt) for c in cases]
+            plain_s = time.perf_counter() - t0
+            line["plain"] = {"sample": f"all {n} integrals, one pg_integrate call each (one pass)",
+                             "plain_integrals_per_s": sum(1 for c, r in zip(cases, pres) if within(c, r)) / plain_s,
+                             "plain_seconds": plain_s, "batched_seconds_per_step": step_s,
+                             "batched_over_plain": plain_s / step_s}
+        elif left > step_s + args.cpu_seconds + 30.0:
+            idx = np.random.default_rng(7).permutation(n)
+            t0 = time.perf_counter()
+            pts, done = 0.0, 0
+            for i in idx:
+                if time.perf_counter() - t0 > 0.5 * step_s:
+                    break
+                c = cases[i]
+                ctx.integrate(c.integrand, c.epsrel, 0.0, options=popt)
+                pts += screen["neval"][i]
+                done += 1
+            plain_s = (time.perf_counter() - t0) * tot_pts / max(pts, 1.0)
+            line["plain"] = {"sample": f"{done} integrals in a seeded random order, time extrapolated to the "
+                                       f"workload by evaluation count",
+                             "plain_seconds_estimated": plain_s, "batched_seconds_per_step": step_s,
+                             "batched_over_plain": plain_s / step_s}
+        else:
+            line["plain"] = {"skipped": f"time budget ({args.time_budget:.0f} s) spent"}
         # CPU baseline: the oracle on all host cores, bounded sample, extrapolated by evaluation count.
-        cpu = cpu_leg(cases, args.cpu_seconds)
-        total_pts = sum(r.neval for r in results)
-        line["cpu_baseline"] = {"value": n / (total_pts / cpu["points_per_s"]), "unit": "integrals/s",
-                                "cores": cpu["threads"], "kind": "port",
-                                "sample": f"first {cpu['integrals']} integrals with <= {CPU_SAMPLE_MAX_REGIONS} regions "
-                                          f"({cpu['seconds']:.1f} s), throughput extrapolated to the whole step "
-                                          f"by evaluation count"}
+        left = args.time_budget - (time.perf_counter() - t_begin)
+        if left > args.cpu_seconds + 10.0:
+            idx = cpu_sample(cases, screen, max(1e8, 2e9 * args.cpu_seconds / 20.0))
+            cpu = cpu_leg(cases, idx)
+            line["cpu_baseline"] = {"value": n / (tot_pts / cpu["points_per_s"]), "unit": "integrals/s",
+                                    "cores": cpu["threads"], "kind": "port",
+                                    "sample": f"{cpu['integrals']} integrals of the workload ({cpu['points']:.3g} rule "
+                                              f"points, {cpu['seconds']:.1f} s, point by point), throughput "
+                                              f"extrapolated to the whole step by evaluation count"}
+        else:
+            line["cpu_baseline"] = {"value": None, "skipped": "time budget spent"}
+        line["wall_s_total"] = time.perf_counter() - t_begin
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def main():
+    t_begin = time.perf_counter()
+    args = parse()
+    if args.config == "5" and args.impl == "gb300":
+        return run_served(args)
+    if args.config == "3" and args.impl == "gb300":
+        return run_mcubes(args)
+    if args.config == "eval":
+        return run_eval(args)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        from gpuintegration_gb300 import workloads as W
+        run_reference(args, W.config4_cases(args.count) if rank == 0 else [], rank, world)
+        return
+    run_batched(args, rank, world, local, t_begin)
 
 
 if __name__ == "__main__":

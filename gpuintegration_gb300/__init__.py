@@ -38,6 +38,11 @@ PG_CUDA_ERROR = -3
 PG_TIMEOUT = -4
 PG_UNSUPPORTED = -5
 
+# Region-evaluation modes (pg_options.eval_mode): every rule point in the
+# reference's order, or generator-set sums for the product-form families.
+EVAL_POINTS = 0
+EVAL_SET_SUMS = 1
+
 CONSTANT, OSCILLATORY, PRODUCT_PEAK, CORNER_PEAK, GAUSSIAN, C0, DISCONTINUOUS, PRODUCT, NAN_VALUE, BOX, FUN6 = range(11)
 FAMILY_NAMES = {
     CONSTANT: "constant", OSCILLATORY: "oscillatory", PRODUCT_PEAK: "product_peak", CORNER_PEAK: "corner_peak",
@@ -71,7 +76,8 @@ class PgStats(ctypes.Structure):
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("tune_warps", ctypes.c_int32 * 2), ("tune_ctas_per_sm", ctypes.c_int32 * 2),
                 ("eval_bytes", ctypes.c_uint64), ("host_ms", ctypes.c_double), ("sync_ms", ctypes.c_double),
-                ("spill_ms", ctypes.c_double), ("admit_ms", ctypes.c_double)]
+                ("spill_ms", ctypes.c_double), ("admit_ms", ctypes.c_double),
+                ("setsum_regions", ctypes.c_uint64)]
 
 
 class PgMcubesOptions(ctypes.Structure):

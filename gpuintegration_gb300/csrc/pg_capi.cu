@@ -227,7 +227,8 @@ static int run_single(pg_context* ctx, const pg::IntegralDesc& D, double epsrel,
   jobs[0].epsrel = epsrel;
   jobs[0].epsabs = epsabs;
   if (opt) jobs[0].opt = *opt; else pg_options_default(&jobs[0].opt);
-  if (jobs[0].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+  if (jobs[0].opt.eval_mode != PG_EVAL_POINTS && jobs[0].opt.eval_mode != PG_EVAL_SET_SUMS)
+    return set_err(ctx, PG_BAD_ARG, "eval_mode must be PG_EVAL_POINTS or PG_EVAL_SET_SUMS");
   if (jobs[0].opt.max_iters <= 0) jobs[0].opt.max_iters = 700;
   if (n) {
     if (!left || !length) return set_err(ctx, PG_BAD_ARG, "null region list");
@@ -304,7 +305,8 @@ int pg_batch_integrate_timed(pg_context* ctx, uint64_t count, const pg_integrand
     jobs[i].epsrel = epsrel[i];
     jobs[i].epsabs = epsabs[i];
     if (opt) jobs[i].opt = *opt; else pg_options_default(&jobs[i].opt);
-    if (jobs[i].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+    if (jobs[i].opt.eval_mode != PG_EVAL_POINTS && jobs[i].opt.eval_mode != PG_EVAL_SET_SUMS)
+      return set_err(ctx, PG_BAD_ARG, "eval_mode must be PG_EVAL_POINTS or PG_EVAL_SET_SUMS");
     if (jobs[i].opt.max_iters <= 0) jobs[i].opt.max_iters = 700;
   }
   pg::RunPolicy pol;
@@ -337,7 +339,8 @@ int pg_serve(pg_context* ctx, uint64_t count, const pg_integrand* fs, const doub
     jobs[i].epsrel = epsrel[i];
     jobs[i].epsabs = epsabs[i];
     if (opt) jobs[i].opt = *opt; else pg_options_default(&jobs[i].opt);
-    if (jobs[i].opt.eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+    if (jobs[i].opt.eval_mode != PG_EVAL_POINTS && jobs[i].opt.eval_mode != PG_EVAL_SET_SUMS)
+      return set_err(ctx, PG_BAD_ARG, "eval_mode must be PG_EVAL_POINTS or PG_EVAL_SET_SUMS");
     if (jobs[i].opt.max_iters <= 0) jobs[i].opt.max_iters = 700;
   }
   pg::RunPolicy pol;
@@ -358,13 +361,14 @@ int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const dou
                                uint64_t n, const double* d_left, const double* d_length, double* d_est, double* d_err,
                                int32_t* d_bisect, int32_t eval_mode) {
   if (!ctx || !f) return set_err(ctx, PG_BAD_ARG, "null argument");
-  if (eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+  if (eval_mode != PG_EVAL_POINTS && eval_mode != PG_EVAL_SET_SUMS)
+    return set_err(ctx, PG_BAD_ARG, "eval_mode must be PG_EVAL_POINTS or PG_EVAL_SET_SUMS");
   Guard g(ctx);
   pg::IntegralDesc D;
   std::string why;
   int rc = pg::prepare_desc(*f, lows, highs, &D, &why);
   if (rc != PG_OK) return set_err(ctx, rc, why);
-  rc = ctx->eng->evaluate(D, n, d_left, d_length, n, d_est, d_err, d_bisect, pg::launch_family_eval);
+  rc = ctx->eng->evaluate(D, n, d_left, d_length, n, d_est, d_err, d_bisect, pg::launch_family_eval, eval_mode);
   if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
   return PG_OK;
 }
@@ -372,7 +376,7 @@ int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const dou
 // Host-buffer region evaluation shared by the family and user-integrand entry points.
 static int evaluate_host(pg_context* ctx, const pg::IntegralDesc& D, uint64_t n, const double* left,
                          const double* length, double* est, double* err, int32_t* bisect,
-                         const pg::EvalLauncher& launch) {
+                         const pg::EvalLauncher& launch, int mode = PG_EVAL_POINTS) {
   int rc;
   if (n == 0) return PG_OK;
   const size_t nd = n * (size_t)D.d;
@@ -385,7 +389,7 @@ static int evaluate_host(pg_context* ctx, const pg::IntegralDesc& D, uint64_t n,
   CAPI_TRY(ctx, cudaMemcpyAsync(ctx->s_left.p, left, nd * 8, cudaMemcpyHostToDevice, s), "upload");
   CAPI_TRY(ctx, cudaMemcpyAsync(ctx->s_len.p, length, nd * 8, cudaMemcpyHostToDevice, s), "upload");
   rc = ctx->eng->evaluate(D, n, (const double*)ctx->s_left.p, (const double*)ctx->s_len.p, n, (double*)ctx->s_est.p,
-                          (double*)ctx->s_err.p, (int32_t*)ctx->s_bis.p, launch);
+                          (double*)ctx->s_err.p, (int32_t*)ctx->s_bis.p, launch, mode);
   if (rc != PG_OK) return set_err(ctx, rc, ctx->eng->last_error);
   CAPI_TRY(ctx, cudaMemcpyAsync(est, ctx->s_est.p, n * 8, cudaMemcpyDeviceToHost, s), "download");
   CAPI_TRY(ctx, cudaMemcpyAsync(err, ctx->s_err.p, n * 8, cudaMemcpyDeviceToHost, s), "download");
@@ -401,13 +405,14 @@ int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lo
                         int32_t eval_mode) {
   if (!ctx || !f || (n && (!left || !length || !est || !err || !bisect)))
     return set_err(ctx, PG_BAD_ARG, "null argument");
-  if (eval_mode != 0) return set_err(ctx, PG_BAD_ARG, "eval_mode must be 0");
+  if (eval_mode != PG_EVAL_POINTS && eval_mode != PG_EVAL_SET_SUMS)
+    return set_err(ctx, PG_BAD_ARG, "eval_mode must be PG_EVAL_POINTS or PG_EVAL_SET_SUMS");
   Guard g(ctx);
   pg::IntegralDesc D;
   std::string why;
   int rc = pg::prepare_desc(*f, lows, highs, &D, &why);
   if (rc != PG_OK) return set_err(ctx, rc, why);
-  return evaluate_host(ctx, D, n, left, length, est, err, bisect, pg::launch_family_eval);
+  return evaluate_host(ctx, D, n, left, length, est, err, bisect, pg::launch_family_eval, eval_mode);
 }
 
 // ---------------------------------------------------------------------------

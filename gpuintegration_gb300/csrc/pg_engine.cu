@@ -1,5 +1,6 @@
 // Host engine of the GB300 PAGANI iteration (see pg_engine.h).
 #include "pg_engine.h"
+#include "pg_setsum.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -353,7 +354,8 @@ void Engine::record(cudaEvent_t a, cudaEvent_t b, double* acc) {
 }
 
 int Engine::evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length,
-                     uint64_t stride, double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch) {
+                     uint64_t stride, double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch,
+                     int mode) {
   int rc;
   if ((rc = autotune()) != PG_OK) return rc;
   if ((rc = ensure(descs_, sizeof(IntegralDesc))) != PG_OK) return rc;
@@ -362,11 +364,13 @@ int Engine::evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left,
   const EvalTune& tn = tune[desc.d <= 8 ? 0 : 1];
   EvalLaunch L{d_left, d_length, n, stride, nullptr, (const IntegralDesc*)descs_.p, &rule_, d_est, d_err, d_bisect,
                desc.d, num_sms, stream_, tn.warps, tn.ctas_per_sm};
+  L.mode = (mode == PG_EVAL_SET_SUMS && family_separable(desc.family)) ? PG_EVAL_SET_SUMS : PG_EVAL_POINTS;
   if (profiling) cudaEventRecord(ev_[0], stream_);
   PG_TRY(launch(L), "evaluation launch");
   stats.launches++;
   stats.eval_launches++;
   stats.regions_evaluated += n;
+  if (L.mode == PG_EVAL_SET_SUMS) stats.setsum_regions += n;
   stats.points_evaluated += n * (uint64_t)rule_.feval[desc.d];
   stats.eval_bytes += n * (16ull * desc.d + 20ull);  // bounds in; estimate, error, split axis out
   if (profiling) {
@@ -559,6 +563,50 @@ int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int max
   return PG_OK;
 }
 
+int Engine::evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& live, int cur, uint64_t N,
+                          const EvalLauncher& launch) {
+  // Runs: maximal ranges of consecutive segments whose integrals share an
+  // evaluation kernel (placement keeps the kernels' integrals together, so an
+  // iteration has a handful of runs).
+  struct Run {
+    uint64_t start, n;
+    int mode, maxd;
+  };
+  std::vector<uint32_t> order(live);
+  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return jobs[a].start < jobs[b].start; });
+  std::vector<Run> runs;
+  for (uint32_t j : order) {
+    const Job& J = jobs[j];
+    if (J.n == 0) continue;
+    const int md = job_eval_mode(J);
+    if (!runs.empty() && runs.back().mode == md && runs.back().start + runs.back().n == J.start) {
+      runs.back().n += J.n;
+      runs.back().maxd = std::max(runs.back().maxd, J.desc.d);
+    } else {
+      runs.push_back(Run{J.start, J.n, md, J.desc.d});
+    }
+  }
+  const double* left = (const double*)left_[cur].p;
+  const double* len = (const double*)len_[cur].p;
+  const uint32_t* own = (const uint32_t*)owner_[cur].p;
+  for (const Run& R : runs) {
+    if (R.start + R.n > N) {
+      last_error = "evaluation run outside the region list";
+      return PG_CUDA_ERROR;
+    }
+    const EvalTune& tn = tune[R.maxd <= 8 ? 0 : 1];
+    EvalLaunch L{left + R.start, len + R.start, R.n, reg_cap_[cur], own + R.start, (const IntegralDesc*)descs_.p,
+                 &rule_, (double*)est_.p + R.start, (double*)err_a_.p + R.start, (int32_t*)bisect_.p + R.start,
+                 R.maxd, num_sms, stream_, tn.warps, tn.ctas_per_sm};
+    L.mode = R.mode;
+    PG_TRY(launch(L), "evaluation launch");
+    stats.launches++;
+    stats.eval_launches++;
+    if (R.mode == PG_EVAL_SET_SUMS) stats.setsum_regions += R.n;
+  }
+  return PG_OK;
+}
+
 int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPolicy& policy) {
   int rc;
   PG_TRY(cudaSetDevice(device), "cudaSetDevice");
@@ -659,26 +707,37 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       uint32_t* hi = (uint32_t*)h_adm_ids_.p;
       std::vector<uint32_t> restore, custom;
       while (first_waiting < njobs && jobs[first_waiting].state == JOB_DONE) ++first_waiting;
+      std::vector<uint32_t> admitted;
       for (uint32_t j = first_waiting; j < njobs; ++j) {
         Job& J = jobs[j];
         if (J.state != JOB_PENDING && J.state != JOB_SPILLED) continue;
         if (J.state == JOB_PENDING && policy.arrival_ms && policy.arrival_ms[j] > now_admit) break;  // not yet arrived
         if (t + J.n > admit_limit && t > 0) break;
-        J.start = t;
-        J.par_start = pp;
         t += J.n;
-        if (J.state == JOB_SPILLED) {
-          pp += J.n / 2;
-          restore.push_back(j);
-        } else if (J.init_n) {
-          custom.push_back(j);
-        } else {
-          hs[adm_pending.size()] = J.start;
-          hi[adm_pending.size()] = j;
-          adm_pending.push_back(j);
-        }
-        J.state = JOB_RESIDENT;
+        admitted.push_back(j);
       }
+      // Placement of the admitted integrals: those evaluated by generator-set
+      // sums first, then the others, so each evaluation kernel sees few runs.
+      t = T;
+      for (int pass = 0; pass < 2; ++pass)
+        for (uint32_t j : admitted) {
+          Job& J = jobs[j];
+          if ((job_eval_mode(J) == PG_EVAL_SET_SUMS) != (pass == 0)) continue;
+          J.start = t;
+          J.par_start = pp;
+          t += J.n;
+          if (J.state == JOB_SPILLED) {
+            pp += J.n / 2;
+            restore.push_back(j);
+          } else if (J.init_n) {
+            custom.push_back(j);
+          } else {
+            hs[adm_pending.size()] = J.start;
+            hi[adm_pending.size()] = j;
+            adm_pending.push_back(j);
+          }
+          J.state = JOB_RESIDENT;
+        }
       if (t > T) {
         if ((rc = grow_list(cur, t, maxd, T, P)) != PG_OK) return rc;
         if (profiling) {
@@ -800,18 +859,12 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     PG_TRY(cudaMemcpyAsync(live_.p, hl, live.size() * 4, cudaMemcpyHostToDevice, stream_), "live upload");
     stats.h2d_bytes += njobs * sizeof(SegDesc) + nchunks * sizeof(ChunkRef) + live.size() * 4;
     // 1. evaluation
-    const EvalTune& tn = tune[maxd <= 8 ? 0 : 1];
-    EvalLaunch L{(const double*)left_[cur].p, (const double*)len_[cur].p, N, reg_cap_[cur],
-                 (const uint32_t*)owner_[cur].p, (const IntegralDesc*)descs_.p, &rule_, (double*)est_.p,
-                 (double*)err_a_.p, (int32_t*)bisect_.p, maxd, num_sms, stream_, tn.warps, tn.ctas_per_sm};
     if (decision_open) {
       stats.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_decision).count();
       decision_open = false;
     }
     if (profiling) cudaEventRecord(ev_[0], stream_);
-    PG_TRY(launch(L), "evaluation launch");
-    stats.launches++;
-    stats.eval_launches++;
+    if ((rc = evaluate_list(jobs, live, cur, N, launch)) != PG_OK) return rc;
     stats.regions_evaluated += N;
     for (uint32_t j : live) {
       stats.points_evaluated += jobs[j].n * (uint64_t)rule_.feval[jobs[j].desc.d];
@@ -947,14 +1000,18 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       }
     // ---- placement of the next list: in order, while the pool has room;
     // the rest leave the pool with their next list in host memory.
+    // Integrals evaluated by generator-set sums are placed first, then the
+    // others, so each evaluation kernel sees few runs of the list.
     Transition* ht = (Transition*)h_trans_.p;
     uint64_t out_total = 0, par_total = 0;
     std::vector<uint32_t> spill;
-    for (uint32_t j = 0; j < njobs; ++j) {
-      Transition Tr;
-      std::memset(&Tr, 0, sizeof Tr);
-      Job& J = jobs[j];
-      if (J.state == JOB_RESIDENT && mode[j] != 0) {
+    std::memset(ht, 0, njobs * sizeof(Transition));
+    for (int pass = 0; pass < 2; ++pass)
+      for (uint32_t j = 0; j < njobs; ++j) {
+        Job& J = jobs[j];
+        if (J.state != JOB_RESIDENT || mode[j] == 0) continue;
+        if ((job_eval_mode(J) == PG_EVAL_SET_SUMS) != (pass == 0)) continue;
+        Transition& Tr = ht[j];
         Tr.mode = mode[j];
         Tr.A = keepA[j];
         if (out_total + 2 * keepA[j] <= cap || out_total == 0) {
@@ -966,8 +1023,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
           spill.push_back(j);
         }
       }
-      ht[j] = Tr;
-    }
+    // Spill groups are formed in integral order (their chunks are contiguous).
+    std::sort(spill.begin(), spill.end());
     // Spilled integrals, in groups of at most one pool's worth of regions:
     // the children of a group go to a transient device buffer in one
     // compaction (integral j at its own offset, rows `stride` apart) and from
@@ -1168,6 +1225,7 @@ int Engine::autotune() {
 // ---------------------------------------------------------------------------
 cudaError_t launch_family_eval(const EvalLaunch& L) {
   const pg_eval_args a = eval_args_of(L);
+  if (L.mode == PG_EVAL_SET_SUMS) return launch_setsum(a);
   return L.maxd <= 8 ? launch_eval<8>(a, FamilyFn{}) : launch_eval<16>(a, FamilyFn{});
 }
 

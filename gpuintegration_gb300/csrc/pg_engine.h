@@ -38,6 +38,7 @@ struct EvalLaunch {
   cudaStream_t stream;
   int warps;        // regions per block (warps per CTA)
   int ctas_per_sm;  // grid cap of the grid-stride evaluation loop
+  int mode = 0;     // 0: point-by-point rule sums (eval_kernel); 1: generator-set sums (setsum_kernel)
 };
 
 // Launch shape of the evaluation kernel for one kernel class (d <= 8, d > 8),
@@ -169,6 +170,13 @@ struct RunPolicy {
   double deadline_ms = 0;
 };
 
+// Evaluation kernel of a job: the generator-set sums when the options ask for
+// them and the integrand is a product of per-axis factors, else point by point.
+inline int job_eval_mode(const Job& J) {
+  return (J.opt.eval_mode == PG_EVAL_SET_SUMS && family_separable(J.desc.family)) ? PG_EVAL_SET_SUMS
+                                                                                   : PG_EVAL_POINTS;
+}
+
 // Prepares an IntegralDesc from the C ABI description (host, no contraction).
 int prepare_desc(const pg_integrand& f, const double* lows, const double* highs, IntegralDesc* out, std::string* why);
 
@@ -191,7 +199,7 @@ class Engine {
 
   // Evaluates caller-given regions (device pointers, SoA stride n).
   int evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left, const double* d_length, uint64_t stride,
-               double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch);
+               double* d_est, double* d_err, int32_t* d_bisect, const EvalLauncher& launch, int mode = 0);
 
   // Times the candidate launch shapes of the evaluation kernel on a synthetic
   // region list per kernel class and keeps the fastest (once per context).
@@ -221,6 +229,10 @@ class Engine {
   int grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_t live_par);
   int compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
               uint64_t out_stride, uint32_t* out_owner, double* parent_out);
+  // Launches the evaluation of list `cur`'s regions [0, N): one launch per
+  // maximal range of resident integrals that share an evaluation kernel.
+  int evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& live, int cur, uint64_t N,
+                    const EvalLauncher& launch);
   void record(cudaEvent_t a, cudaEvent_t b, double* acc);
 
   cudaStream_t stream_ = nullptr;

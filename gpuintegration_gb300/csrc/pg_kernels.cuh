@@ -447,6 +447,9 @@ static __global__ void uniform_split_batch_kernel(double* __restrict__ left, dou
   const int parts = d < 5 ? 4 : (d <= 10 ? 2 : 1);
   const double len = __ddiv_rn(1.0, (double)parts);
   uint64_t q = r - starts[lo];
+  uint64_t total = 1;
+  for (int k = 0; k < d; ++k) total *= (uint64_t)parts;
+  if (q >= total) return;  // a gap held by another admitted integral
   for (int k = 0; k < d; ++k) {
     const uint64_t id = q % (uint64_t)parts;
     q /= (uint64_t)parts;

@@ -97,6 +97,22 @@ typedef struct pg_result {
   int32_t last_phase; /* -1 as in the reference */
 } pg_result;
 
+/* Region-evaluation modes (pg_options.eval_mode, pg_evaluate_regions' eval_mode).
+ * PG_EVAL_POINTS evaluates every point of the degree-9 rule and accumulates
+ * the five rule sums point by point in the reference's order
+ * (cuda/pagani/quad/GPUquad/Sample.cuh:103-290): estimates, errors and split
+ * axes are bit-identical to the reference's own kernel.
+ * PG_EVAL_SET_SUMS applies to the product-form families (PRODUCT_PEAK,
+ * GAUSSIAN, C0, DISCONTINUOUS, PRODUCT) and falls back to PG_EVAL_POINTS for
+ * the others: the nine generator-set sums of f are formed by a recurrence over
+ * the axes from the 11 per-axis factor values, so a region costs O(ndim)
+ * instead of FEVAL(ndim) point values.  Estimates and errors agree with
+ * PG_EVAL_POINTS to about 1e-15 of the region's estimate (the rounding of the
+ * sums differs); the split axes are the reference's, because the values the
+ * fourth differences read are formed exactly as PG_EVAL_POINTS forms them. */
+#define PG_EVAL_POINTS 0
+#define PG_EVAL_SET_SUMS 1
+
 /* Options of the PAGANI iteration.  pg_options_default() gives the reference's
  * behaviour: relative-error classification on (Workspace.cuh:360-368), 700
  * iterations (Workspace.cuh:399), and the heuristic classifier's device-memory
@@ -106,7 +122,7 @@ typedef struct pg_options {
   int32_t max_iters;
   double device_mem_model;  /* bytes seen by the memory-pressure classifier */
   uint64_t max_regions;     /* hard cap of the region pool (0 = derived from the model) */
-  int32_t eval_mode;        /* must be 0: per-region rule sums in the reference's order */
+  int32_t eval_mode;        /* PG_EVAL_POINTS (default) or PG_EVAL_SET_SUMS */
   int32_t predict_split;    /* 1: the reference's predict_split variant (Workspace.cuh:415-441): no rel-err
                                classification in the first 15 iterations while the list has <= 15e6 regions and
                                nothing has finished; the list of iteration 15 is kept (pg_last_snapshot) */
@@ -132,6 +148,7 @@ typedef struct pg_stats {
   double sync_ms;               /* host time blocked waiting for an iteration's device work */
   double spill_ms;              /* device time of moving region lists out of the pool (compaction + copies) */
   double admit_ms;              /* device time of admissions: first splits and region lists moved back in */
+  uint64_t setsum_regions;      /* regions evaluated by generator-set sums (PG_EVAL_SET_SUMS) */
 } pg_stats;
 
 void pg_options_default(pg_options* opt);
@@ -178,7 +195,7 @@ int pg_last_snapshot(pg_context* ctx, int32_t* ndim, uint64_t* n, double* left, 
  * stage tests call directly (test/cuda/pagani/RegionSampling.cu:48-88). */
 int pg_evaluate_regions(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,
                         uint64_t n, const double* left, const double* length, double* est, double* err,
-                        int32_t* bisect, int32_t eval_mode /* must be 0 */);
+                        int32_t* bisect, int32_t eval_mode /* PG_EVAL_POINTS or PG_EVAL_SET_SUMS */);
 
 /* Same on device buffers, asynchronous on the context stream. */
 int pg_evaluate_regions_device(pg_context* ctx, const pg_integrand* f, const double* lows, const double* highs,

@@ -44,6 +44,8 @@ def load():
     P = ctypes.POINTER
     vp = ctypes.c_void_p
     lib.orc_feval.restype = ctypes.c_int
+    lib.orc_set_eval_mode.argtypes = [ctypes.c_int]
+    lib.orc_set_eval_mode.restype = ctypes.c_int
     lib.orc_rule_tables.argtypes = [ctypes.c_int, _D, _D, _D, P(ctypes.c_int32), _D]
     lib.orc_eval_point.restype = ctypes.c_double
     lib.orc_eval_point.argtypes = [vp, _D]
@@ -98,6 +100,21 @@ def eval_point(f, x):
     x = np.ascontiguousarray(x, dtype=np.float64)
     s = _integrand_struct(f)
     return lib.orc_eval_point(ctypes.byref(s), _p(x))
+
+
+class eval_mode:
+    """Context manager: the oracle's region-evaluation mode inside the block
+    (0 point by point, 1 generator-set sums for the product-form families)."""
+
+    def __init__(self, mode):
+        self.mode = mode
+
+    def __enter__(self):
+        assert load().orc_set_eval_mode(self.mode) == 0
+        return self
+
+    def __exit__(self, *a):
+        load().orc_set_eval_mode(0)
 
 
 def evaluate_regions(f, left, length, lows=None, highs=None, nthreads=None):

@@ -504,6 +504,134 @@ static EvalOut eval_region(const Rule& R, const Prepared& P, const double* lows,
   return o;
 }
 
+// ---------------------------------------------------------------------------
+// Region evaluation by generator-set sums (the library's PG_EVAL_SET_SUMS
+// mode) for integrands that are products of per-axis factors.  Each rule sum
+// is sum_s w[s][r] * S_s with S_s the sum of f over generator set s
+// (Sample.cuh:145-148 accumulates f * w[set(p)][r] point by point); for
+// f = prod_k h_k(x_k) the nine S_s follow from a recurrence over the axes on
+// the 11 factor values h_k(centre), h_k(+-G_t).  The 4d+1 point values of the
+// fourth differences (Sample.cuh:190-215) are formed exactly as eval() forms
+// them (two half products in axis order), so the split axis is the
+// point-by-point evaluation's.  Operation for operation the library's
+// setsum_kernel.
+// ---------------------------------------------------------------------------
+static bool product_form(int family) {
+  return family == FAM_PRODUCT_PEAK || family == FAM_GAUSSIAN || family == FAM_C0 || family == FAM_DISCONTINUOUS ||
+         family == FAM_PRODUCT;
+}
+
+static EvalOut eval_region_setsums(const Rule& R, const Prepared& P, const double* lows, const double* highs,
+                                   const double* lower, const double* length) {
+  const int d = R.ndim;
+  double jac = 1.0;
+  for (int k = 0; k < d; ++k) jac = jac * (highs[k] - lows[k]);
+  double A[11], B[11];
+  A[0] = .5 + 0.0;
+  B[0] = .5 - 0.0;
+  for (int t = 0; t < 5; ++t) {
+    A[1 + t] = .5 + R.G[t];
+    B[1 + t] = .5 - R.G[t];
+    A[6 + t] = .5 + -R.G[t];
+    B[6 + t] = .5 - -R.G[t];
+  }
+  double e0 = 1.0, a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, b = 0.0, g = 0.0, t3 = 0.0, z = 1.0;
+  double vol = 1.0, widest = 0.0;
+  int maxdim = 0;
+  double fv[kMaxDim][5];  // centre, +G0, -G0, +G1, -G1
+  for (int k = 0; k < d; ++k) {
+    const double lo = lower[k], up = lo + length[k];
+    const double side = up - lo;
+    if (side > widest) {
+      widest = side;
+      maxdim = k;
+    }
+    vol = (k == 0) ? side : vol * side;
+    const double glo = lows[k], range = highs[k] - lows[k];
+    double h[11];
+    for (int c = 0; c < 11; ++c) {
+      const double t = std::fma(A[c], lo, B[c] * up);
+      const double x = std::fma(t, range, glo);
+      h[c] = (P.family == FAM_PRODUCT) ? x : factor(P, k, x);
+    }
+    fv[k][0] = h[0];
+    fv[k][1] = h[1];
+    fv[k][2] = h[6];
+    fv[k][3] = h[2];
+    fv[k][4] = h[7];
+    const double c = h[0];
+    const double p0 = h[1] + h[6], p1 = h[2] + h[7], p2 = h[3] + h[8], p3 = h[4] + h[9], p4 = h[5] + h[10];
+    t3 = std::fma(b, p0, t3 * c);
+    g = std::fma(a1, p0, std::fma(a0, p1, g * c));
+    b = std::fma(a0, p0, b * c);
+    a0 = std::fma(e0, p0, a0 * c);
+    a1 = std::fma(e0, p1, a1 * c);
+    a2 = std::fma(e0, p2, a2 * c);
+    a3 = std::fma(e0, p3, a3 * c);
+    e0 = e0 * c;
+    z = z * p4;
+  }
+  const bool scale_jac = jac != 1.0;
+  const double S[kNSets] = {e0, a0, a1, a2, a3, b, g, t3, z};
+  double s5[kNRules];
+  for (int q = 0; q < kNRules; ++q) {
+    double v = R.w[q] * S[0];
+    for (int st = 1; st < kNSets; ++st) v = std::fma(R.w[st * kNRules + q], S[st], v);
+    s5[q] = scale_jac ? v * jac : v;
+  }
+  // Fourth differences from the exact point values.
+  const int m = d / 2;
+  double Lc = fv[0][0], Rc = fv[m][0];
+  for (int k = 1; k < m; ++k) Lc = Lc * fv[k][0];
+  for (int k = m + 1; k < d; ++k) Rc = Rc * fv[k][0];
+  double f0 = Lc * Rc;
+  if (scale_jac) f0 = f0 * jac;
+  const double f02 = f0 + f0;
+  const double q = R.G[1] / R.G[0];
+  const double ratio = q * q, omr = 1 - ratio;
+  double maxdiff = 0;
+  int bisect = maxdim;
+  double pre = 1.0;
+  for (int k = 0; k < d; ++k) {
+    const bool lhalf = k < m;
+    const int hbeg = lhalf ? 0 : m, hend = lhalf ? m : d;
+    double f[4];
+    for (int v = 0; v < 4; ++v) {
+      double Pv = (k == hbeg) ? fv[k][1 + v] : pre * fv[k][1 + v];
+      for (int j = k + 1; j < hend; ++j) Pv = Pv * fv[j][0];
+      const double fp = lhalf ? Pv * Rc : Lc * Pv;
+      f[v] = scale_jac ? fp * jac : fp;
+    }
+    pre = (k == hbeg) ? fv[k][0] : pre * fv[k][0];
+    if (k + 1 == m) pre = 1.0;
+    const double X = f[0] + f[1], Y = f[2] + f[3];
+    const double s = (d <= 4) ? std::fma(f02, omr, ratio * X) : std::fma(ratio, X, f02 * omr);
+    const double fd = std::fabs(s - Y);
+    if (fd > maxdiff) {
+      maxdiff = fd;
+      bisect = k;
+    }
+  }
+  // Null-rule error (Sample.cuh:261-289).
+  double e[3];
+  for (int r = 1; r < kNRules - 1; ++r) {
+    double maxerr = 0.;
+    for (int st = 0; st < kNSets; ++st)
+      maxerr = std::fmax(maxerr, std::fabs(std::fma(R.scale[st * kNRules + r], s5[r], s5[r + 1])) *
+                                     R.norm[st * kNRules + r]);
+    e[r - 1] = maxerr;
+  }
+  EvalOut o;
+  o.est = vol * s5[0];
+  o.err = vol * ((5. * e[0] <= e[1] && 5. * e[1] <= e[2]) ? e[0] : 5. * std::fmax(std::fmax(e[0], e[1]), e[2]));
+  o.bisect = bisect;
+  return o;
+}
+
+// Evaluation mode of the oracle's evaluate_all: 0 point by point (the
+// reference's order), 1 generator-set sums for the product-form families.
+static int g_eval_mode = 0;
+
 static void parallel_for(size_t n, int nthreads, const std::function<void(size_t, size_t)>& body) {
   if (nthreads <= 1 || n < 64) {
     body(0, n);
@@ -530,7 +658,8 @@ static void evaluate_all(const Rule& R, const Prepared& P, const double* lows, c
         lo[k] = left[(size_t)k * n + i];
         ln[k] = len[(size_t)k * n + i];
       }
-      const EvalOut o = eval_region(R, P, lows, highs, lo, ln);
+      const EvalOut o = (g_eval_mode == 1 && product_form(P.family)) ? eval_region_setsums(R, P, lows, highs, lo, ln)
+                                                                     : eval_region(R, P, lows, highs, lo, ln);
       est[i] = o.est;
       err[i] = o.err;
       bis[i] = o.bisect;
@@ -721,6 +850,14 @@ typedef struct {
 } orc_result;
 
 int orc_feval(int ndim) { return orc::feval_count(ndim); }
+
+// Region-evaluation mode of every later evaluation and integration call:
+// 0 point by point, 1 generator-set sums for the product-form families.
+int orc_set_eval_mode(int mode) {
+  if (mode != 0 && mode != 1) return -1;
+  orc::g_eval_mode = mode;
+  return 0;
+}
 
 // Rule tables: w/scale/norm [45], set_of [feval], gen [feval*ndim] (point-major).
 int orc_rule_tables(int ndim, double* w, double* scale, double* norm, int32_t* set_of, double* gen) {
