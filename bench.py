@@ -70,9 +70,10 @@ def parse():
     p.add_argument("--time-budget", type=float, default=1500.0,
                    help="seconds the whole run may take; legs after the timed steps shrink or are skipped to fit")
     p.add_argument("--max-regions", type=int, default=1 << 26)
-    p.add_argument("--config", default="4", choices=["3", "4", "5", "eval"],
+    p.add_argument("--config", default="4", choices=["3", "4", "5", "eval", "single"],
                    help="4: batched workload (default, the metric's configuration); 5: served workload; "
-                        "3: m-Cubes Gaussian; eval: one evaluation kernel on a synthetic region list")
+                        "3: m-Cubes Gaussian; eval: one evaluation kernel on a synthetic region list; "
+                        "single: one integral of the workload through the plain path")
     p.add_argument("--rate", type=float, default=2000.0, help="config 5: Poisson arrival rate (requests/s)")
     p.add_argument("--duration", type=float, default=60.0, help="config 5: arrival window (s)")
     p.add_argument("--budget-gb", type=float, default=120.0, help="config 5: device budget of the region pool")
@@ -81,6 +82,8 @@ def parse():
     p.add_argument("--family", default="c0", help="config eval: integrand family name")
     p.add_argument("--ndim", type=int, default=8, help="config eval: dimension")
     p.add_argument("--regions", type=int, default=1 << 20, help="config eval: regions per launch")
+    p.add_argument("--index", type=int, default=2069,
+                   help="config single: workload integral (default 2069: 8-D C0, epsrel 4.6e-6, 1.3e7 regions)")
     return p.parse_args()
 
 
@@ -297,6 +300,36 @@ def run_eval(args):
     print(json.dumps(line), flush=True)
 
 
+def run_single(args):
+    """One integral of the batched workload through pg_integrate, with the
+    evaluation launches' CUDA-event time (the kernels as the iteration runs
+    them: after the first iteration the set-sum kernel evaluates siblings in
+    pairs)."""
+    import gpuintegration_gb300 as pg
+    from gpuintegration_gb300 import workloads as W
+    c = W.config4_cases(args.index + 1)[args.index]
+    ctx = pg.Context(0)
+    opt = pg.default_options(eval_mode=EVAL_MODES[args.eval_mode])
+    for _ in range(args.warmup):
+        ctx.integrate(c.integrand, c.epsrel, 0.0, options=opt)
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = ctx.integrate(c.integrand, c.epsrel, 0.0, options=opt)
+    wall = (time.perf_counter() - t0) / args.steps
+    st = ctx.stats()
+    f = c.integrand
+    line = {"metric": "plain PAGANI, one integral", "config": {"workload": f"workload integral {args.index}: "
+            f"{pg.FAMILY_NAMES[f.family]} d={f.ndim} epsrel {c.epsrel:.3g}", "eval_mode": args.eval_mode},
+            "wall_ms": wall * 1000.0, "eval_ms": st.eval_ms / args.steps, "stage_ms": st.stage_ms / args.steps,
+            "host_ms": st.host_ms / args.steps, "regions": st.regions_evaluated // args.steps,
+            "ns_per_region_eval": st.eval_ms * 1e6 / max(st.regions_evaluated, 1),
+            "estimate": r.estimate, "errorest": r.errorest, "status": r.status, "within": within(c, r),
+            "iters": r.iters}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------------
 CPU_SAMPLE_MAX_REGIONS = 200000
 
@@ -416,6 +449,21 @@ def roofline(ctx, cases, results, st, steps, mode):
             "hbm_gbs_of_eval": st.eval_bytes / eval_s / 1e9}
 
 
+def iteration_summary(it, steps):
+    """Evaluation time by the size of the iteration's region list."""
+    out = {"per_step": len(it) / steps, "eval_ms_by_list_size": {}}
+    edges = [0, 10 ** 4, 10 ** 5, 10 ** 6, 10 ** 7, 10 ** 9]
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        sel = (it["regions"] >= lo) & (it["regions"] < hi)
+        if not sel.any():
+            continue
+        ms = float(it["eval_ms"][sel].sum())
+        reg = float(it["regions"][sel].sum())
+        out["eval_ms_by_list_size"][f"[{lo:.0e},{hi:.0e})"] = {
+            "iterations": int(sel.sum()) / steps, "eval_ms": ms / steps, "ns_per_region": 1e6 * ms / max(reg, 1.0)}
+    return out
+
+
 def run_batched(args, rank, world, local, t_begin):
     import torch
     import gpuintegration_gb300 as pg
@@ -495,7 +543,8 @@ def run_batched(args, rank, world, local, t_begin):
             "step_breakdown_ms": {"evaluation": st.eval_ms / args.steps, "stages": st.stage_ms / args.steps,
                                   "host_decisions": st.host_ms / args.steps, "spill": st.spill_ms / args.steps,
                                   "admission": st.admit_ms / args.steps},
-            "setsum_region_share": st.setsum_regions / max(st.regions_evaluated, 1)}
+            "setsum_region_share": st.setsum_regions / max(st.regions_evaluated, 1),
+            "iterations": iteration_summary(ctx.iterations(), args.steps)}
     if rank == 0:
         step_s = wall_s / args.steps
         left = args.time_budget - (time.perf_counter() - t_begin)
@@ -558,6 +607,8 @@ def main():
         return run_mcubes(args)
     if args.config == "eval":
         return run_eval(args)
+    if args.config == "single":
+        return run_single(args)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -80,6 +80,11 @@ class PgStats(ctypes.Structure):
                 ("setsum_regions", ctypes.c_uint64)]
 
 
+class PgIterationRecord(ctypes.Structure):
+    _fields_ = [("regions", ctypes.c_uint64), ("integrals", ctypes.c_uint32), ("eval_launches", ctypes.c_uint32),
+                ("eval_ms", ctypes.c_double), ("stage_ms", ctypes.c_double)]
+
+
 class PgMcubesOptions(ctypes.Structure):
     _fields_ = [("ncall", ctypes.c_double), ("titer", ctypes.c_int32), ("itmax", ctypes.c_int32),
                 ("skip", ctypes.c_int32), ("nbins", ctypes.c_int32), ("seed", ctypes.c_uint64),
@@ -114,6 +119,8 @@ def load_library(path: str = LIB_PATH):
         "pg_context_set_profiling": (ctypes.c_int, [c_ctx, ctypes.c_int]),
         "pg_context_stats": (ctypes.c_int, [c_ctx, P(PgStats)]),
         "pg_context_reset_stats": (ctypes.c_int, [c_ctx]),
+        "pg_context_iterations": (ctypes.c_int, [c_ctx, P(PgIterationRecord), ctypes.c_uint64,
+                                                 P(ctypes.c_uint64)]),
         "pg_context_stream": (ctypes.c_void_p, [c_ctx]),
         "pg_synchronize": (ctypes.c_int, [c_ctx]),
         "pg_integrate_regions": (ctypes.c_int, [c_ctx, P(PgIntegrand), _D, _D, ctypes.c_uint64, ctypes.c_double,
@@ -280,6 +287,17 @@ class Context:
 
     def reset_stats(self):
         self.lib.pg_context_reset_stats(self.h)
+
+    def iterations(self) -> np.ndarray:
+        """Per-iteration records since the last reset_stats (profiling on): a structured
+        array with fields regions, integrals, eval_launches, eval_ms, stage_ms."""
+        n = ctypes.c_uint64()
+        self._check(self.lib.pg_context_iterations(self.h, None, 0, ctypes.byref(n)))
+        buf = (PgIterationRecord * max(n.value, 1))()
+        self._check(self.lib.pg_context_iterations(self.h, buf, n.value, ctypes.byref(n)))
+        dt = np.dtype([("regions", np.uint64), ("integrals", np.uint32), ("eval_launches", np.uint32),
+                       ("eval_ms", np.float64), ("stage_ms", np.float64)])
+        return np.frombuffer(bytes(buf), dtype=dt, count=n.value).copy()
 
     # -- PAGANI -------------------------------------------------------------
     def integrate(self, f: Integrand, epsrel: float, epsabs: float, vol: Optional[Volume] = None,

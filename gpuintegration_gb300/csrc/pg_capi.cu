@@ -199,6 +199,15 @@ int pg_context_stats(const pg_context* ctx, pg_stats* out) {
 int pg_context_reset_stats(pg_context* ctx) {
   if (!ctx) return PG_BAD_ARG;
   ctx->eng->stats = pg_stats{};
+  ctx->eng->iterations.clear();
+  return PG_OK;
+}
+
+int pg_context_iterations(const pg_context* ctx, pg_iteration_record* out, uint64_t capacity, uint64_t* count) {
+  if (!ctx || !count || (capacity && !out)) return PG_BAD_ARG;
+  const auto& it = ctx->eng->iterations;
+  *count = it.size();
+  for (uint64_t i = 0; i < capacity && i < it.size(); ++i) out[i] = it[i];
   return PG_OK;
 }
 

@@ -599,6 +599,8 @@ int Engine::evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& l
                  &rule_, (double*)est_.p + R.start, (double*)err_a_.p + R.start, (int32_t*)bisect_.p + R.start,
                  R.maxd, num_sms, stream_, tn.warps, tn.ctas_per_sm};
     L.mode = R.mode;
+    L.segs = (const SegDesc*)segs_.p;
+    L.base = R.start;
     PG_TRY(launch(L), "evaluation launch");
     stats.launches++;
     stats.eval_launches++;
@@ -864,6 +866,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       decision_open = false;
     }
     if (profiling) cudaEventRecord(ev_[0], stream_);
+    const uint64_t eval_launches0 = stats.eval_launches;
     if ((rc = evaluate_list(jobs, live, cur, N, launch)) != PG_OK) return rc;
     stats.regions_evaluated += N;
     for (uint32_t j : live) {
@@ -893,8 +896,12 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     stats.d2h_bytes += njobs * sizeof(IterScalars);
     stats.stage_bytes += N * 29;
     if (profiling) {
-      record(ev_[0], ev_[1], &stats.eval_ms);
-      record(ev_[1], ev_[2], &stats.stage_ms);
+      pg_iteration_record rec{N, (uint32_t)live.size(), (uint32_t)(stats.eval_launches - eval_launches0), 0.0, 0.0};
+      record(ev_[0], ev_[1], &rec.eval_ms);
+      record(ev_[1], ev_[2], &rec.stage_ms);
+      stats.eval_ms += rec.eval_ms;
+      stats.stage_ms += rec.stage_ms;
+      iterations.push_back(rec);
       if (compact_timing_pending_) record(ev_[2 + 2], ev_[3 + 2], &stats.stage_ms);
       if (spill_timing_pending_) record(ev_[6], ev_[7], &stats.spill_ms);
       if (admit_timing_pending_) record(ev_[8], ev_[9], &stats.admit_ms);
@@ -1225,7 +1232,7 @@ int Engine::autotune() {
 // ---------------------------------------------------------------------------
 cudaError_t launch_family_eval(const EvalLaunch& L) {
   const pg_eval_args a = eval_args_of(L);
-  if (L.mode == PG_EVAL_SET_SUMS) return launch_setsum(a);
+  if (L.mode == PG_EVAL_SET_SUMS) return launch_setsum(a, L.segs, L.base);
   return L.maxd <= 8 ? launch_eval<8>(a, FamilyFn{}) : launch_eval<16>(a, FamilyFn{});
 }
 

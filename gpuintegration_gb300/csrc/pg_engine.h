@@ -39,6 +39,11 @@ struct EvalLaunch {
   int warps;        // regions per block (warps per CTA)
   int ctas_per_sm;  // grid cap of the grid-stride evaluation loop
   int mode = 0;     // 0: point-by-point rule sums (eval_kernel); 1: generator-set sums (setsum_kernel)
+  // Set-sum kernel only: the integrals' segments of the list (siblings are
+  // evaluated together; null: every region alone) and the list position of
+  // left[0].
+  const SegDesc* segs = nullptr;
+  uint64_t base = 0;
 };
 
 // Launch shape of the evaluation kernel for one kernel class (d <= 8, d > 8),
@@ -212,6 +217,7 @@ class Engine {
   cudaStream_t stream() const { return stream_; }
   const RuleDev& rule() const { return rule_; }
   pg_stats stats{};
+  std::vector<pg_iteration_record> iterations;  // while profiling
   bool profiling = false;
   std::string last_error;
   int device = 0;

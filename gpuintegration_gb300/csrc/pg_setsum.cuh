@@ -23,6 +23,19 @@
 // estimates and errors agree with the point-by-point evaluation to ~1e-15 of
 // the region's estimate.
 //
+// The recurrence is a product of per-axis terms, so the axes can be taken in
+// any order.  Each region has a deferred axis s that enters last: the other
+// axes in axis order, then s.  For a region whose sibling is evaluated with it
+// (below) s is the axis the two differ on; otherwise s = d - 1, which is the
+// plain axis order.
+//
+// Siblings: after the first iteration an integral's list holds the two
+// children of its k-th kept region at k and n/2 + k, equal on every axis but
+// the parent's split axis (Sub_region_splitter.cuh:8-46).  One thread
+// evaluates both: the factors of the d - 1 shared axes once, the recurrence
+// over them once, then each child's own factors of the split axis.  At d = 8
+// that is 99 factor evaluations per pair instead of 176.
+//
 // The split axis needs f at the centre and at +-G0, +-G1 on each axis, and it
 // must be the reference's decision exactly, so those 4d+1 values are formed
 // exactly as the point-by-point evaluation forms them: the two half products
@@ -32,18 +45,23 @@
 // (Sample.cuh:190-290, Phases.cuh:329-348) with the same operations as
 // eval_kernel.
 //
-// One thread per region: a region's recurrence is sequential over the axes,
-// and with a thread per region every FP64 warp instruction carries 32
-// regions' work.  Loads of the SoA bounds and stores of the results are
-// coalesced across the warp.
+// One thread per region or sibling pair: with a thread per region every FP64
+// warp instruction carries 32 regions' work, and the SoA loads of the bounds
+// and the stores of the results are coalesced across the warp.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "pg_eval.cuh"
+#include "pg_kernels.cuh"
 
 namespace pg {
+
+// Multiply of the set-sum kernel: the IEEE product on the integer pipe.
+#ifndef PG_SETSUM_MUL
+#define PG_SETSUM_MUL mul_rn_int
+#endif
 
 constexpr int kSetSumThreads = 128;
 constexpr int kFdValues = 5;  // per axis: factor at the centre, +G0, -G0, +G1, -G1
@@ -53,182 +71,272 @@ struct SetSumSmem {
   double w[(MAXD + 1) * 45];
   double scale[(MAXD + 1) * 45];
   double norm[(MAXD + 1) * 45];
-  double fd[kFdValues * MAXD * kSetSumThreads];  // [(k * 5 + v) * threads + thread]
+  double fd[kFdValues * (MAXD + 1) * kSetSumThreads];  // [(k * 5 + v) * threads + thread]; row MAXD: sibling's axis
 };
 
+// Inputs of one axis to the recurrence.
+struct AxisTerm {
+  double c, p0, p1, p2, p3, p4;
+};
+
+// The nine generator-set sums (sets 0..8).
+struct SetSums {
+  double e0, a0, a1, a2, a3, b, g, t3, z;
+};
+
+__device__ __forceinline__ void set_step(SetSums& S, const AxisTerm& A) {
+  S.t3 = __fma_rn(S.b, A.p0, PG_SETSUM_MUL(S.t3, A.c));
+  S.g = __fma_rn(S.a1, A.p0, __fma_rn(S.a0, A.p1, PG_SETSUM_MUL(S.g, A.c)));
+  S.b = __fma_rn(S.a0, A.p0, PG_SETSUM_MUL(S.b, A.c));
+  S.a0 = __fma_rn(S.e0, A.p0, PG_SETSUM_MUL(S.a0, A.c));
+  S.a1 = __fma_rn(S.e0, A.p1, PG_SETSUM_MUL(S.a1, A.c));
+  S.a2 = __fma_rn(S.e0, A.p2, PG_SETSUM_MUL(S.a2, A.c));
+  S.a3 = __fma_rn(S.e0, A.p3, PG_SETSUM_MUL(S.a3, A.c));
+  S.e0 = PG_SETSUM_MUL(S.e0, A.c);
+  S.z = PG_SETSUM_MUL(S.z, A.p4);
+}
+
+// The 11 factor values of axis k over [lo, up] (coordinates as Sample.cuh:126-131
+// forms them); writes the five the fourth differences read to fd[v * T].
+__device__ __forceinline__ AxisTerm axis_term(const IntegralDesc& D, const RuleDev& rule, int k, double lo,
+                                              double up, bool unit, double* fd, int T) {
+  double h[kCodesPerDim];
+#pragma unroll
+  for (int c = 0; c < kCodesPerDim; ++c) {
+    const double t = __fma_rn(rule.A[c], lo, PG_SETSUM_MUL(rule.B[c], up));
+    h[c] = family_factor(D, k, unit ? t : __fma_rn(t, D.range[k], D.glo[k]));
+  }
+  fd[0 * T] = h[0];
+  fd[1 * T] = h[1];
+  fd[2 * T] = h[6];
+  fd[3 * T] = h[2];
+  fd[4 * T] = h[7];
+  return AxisTerm{h[0], __dadd_rn(h[1], h[6]), __dadd_rn(h[2], h[7]), __dadd_rn(h[3], h[8]), __dadd_rn(h[4], h[9]),
+                  __dadd_rn(h[5], h[10])};
+}
+
+// Rule sums, split axis and null-rule error of one region from its set sums.
+// Factor value v of axis k is fv[(k * 5 + v) * T], except on axis `sk`, whose
+// values are at own[v * T].
+template <int MAXD>
+__device__ __forceinline__ void region_result(const SetSumSmem<MAXD>& Sm, const RuleDev& rule, const SetSums& Q,
+                                              int d, double jac, double vol, int maxdim, const double* fv, int sk,
+                                              const double* own, double* est, double* err, int32_t* bisect) {
+  constexpr int T = kSetSumThreads;
+  const bool scale_jac = jac != 1.0;
+  const double* W = Sm.w + d * 45;
+  double s5[kNRules];
+#pragma unroll
+  for (int q = 0; q < kNRules; ++q) {
+    double v = PG_SETSUM_MUL(W[q], Q.e0);
+    v = __fma_rn(W[5 + q], Q.a0, v);
+    v = __fma_rn(W[10 + q], Q.a1, v);
+    v = __fma_rn(W[15 + q], Q.a2, v);
+    v = __fma_rn(W[20 + q], Q.a3, v);
+    v = __fma_rn(W[25 + q], Q.b, v);
+    v = __fma_rn(W[30 + q], Q.g, v);
+    v = __fma_rn(W[35 + q], Q.t3, v);
+    v = __fma_rn(W[40 + q], Q.z, v);
+    s5[q] = scale_jac ? PG_SETSUM_MUL(v, jac) : v;
+  }
+  auto F = [&](int k, int v) -> double { return (k == sk) ? own[v * T] : fv[(k * kFdValues + v) * T]; };
+  // Point values of the fourth differences, formed as the point-by-point
+  // evaluation forms them: L * R from the two half products in axis order.
+  const int m = d / 2;
+  double Lc = F(0, 0), Rc = F(m, 0);
+  for (int k = 1; k < m; ++k) Lc = PG_SETSUM_MUL(Lc, F(k, 0));
+  for (int k = m + 1; k < d; ++k) Rc = PG_SETSUM_MUL(Rc, F(k, 0));
+  double f0 = PG_SETSUM_MUL(Lc, Rc);
+  if (scale_jac) f0 = PG_SETSUM_MUL(f0, jac);
+  const double f02 = __dadd_rn(f0, f0);
+  unsigned long long kmax = 0ull;
+  int cand = -1;
+  double pre = 1.0;  // product of the centre factors of the earlier axes of the current half
+  for (int k = 0; k < d; ++k) {
+    const bool lhalf = k < m;
+    const int hbeg = lhalf ? 0 : m, hend = lhalf ? m : d;
+    // The half product of each of the four points, the four chains side by side.
+    double f[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v] = (k == hbeg) ? F(k, 1 + v) : PG_SETSUM_MUL(pre, F(k, 1 + v));
+    for (int q = k + 1; q < hend; ++q) {
+      const double cq = F(q, 0);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f[v] = PG_SETSUM_MUL(f[v], cq);
+    }
+    const double other = lhalf ? Rc : Lc;  // the other half's centre product
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      f[v] = PG_SETSUM_MUL(f[v], other);
+      if (scale_jac) f[v] = PG_SETSUM_MUL(f[v], jac);
+    }
+    const double ck = F(k, 0);
+    pre = (k == hbeg) ? ck : PG_SETSUM_MUL(pre, ck);
+    if (k + 1 == m) pre = 1.0;
+    // base + ratio*(fp+fm) - (fp2+fm2), base = 2*f0*(1-ratio): the
+    // reference's compiled code fuses the base multiply for d <= 4 and the
+    // ratio multiply for d >= 5 (Sample.cuh:190-215).
+    const double X = __dadd_rn(f[0], f[1]);
+    const double Y = __dadd_rn(f[2], f[3]);
+    const double s = (d <= 4) ? __fma_rn(f02, rule.omr, __dmul_rn(rule.ratio, X))
+                              : __fma_rn(rule.ratio, X, __dmul_rn(f02, rule.omr));
+    const unsigned long long fd = (unsigned long long)__double_as_longlong(fabs(__dsub_rn(s, Y)));
+    if (fd != 0ull && fd <= 0x7ff0000000000000ull && fd > kmax) {
+      kmax = fd;
+      cand = k;
+    }
+  }
+  // Null-rule error (Sample.cuh:261-289): maxima of non-negative terms on
+  // their bit patterns, a NaN term ignored.
+  const double* SC = Sm.scale + d * 45;
+  const double* NM = Sm.norm + d * 45;
+  unsigned long long mq[3] = {0ull, 0ull, 0ull};
+#pragma unroll
+  for (int q = 1; q <= 3; ++q) {
+    unsigned long long mx = 0ull;
+#pragma unroll
+    for (int st = 0; st < kNSets; ++st) {
+      const unsigned long long bt = (unsigned long long)__double_as_longlong(
+          PG_SETSUM_MUL(fabs(__fma_rn(SC[st * kNRules + q], s5[q], s5[q + 1])), NM[st * kNRules + q]));
+      const unsigned long long term = (bt & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : bt;
+      mx = term > mx ? term : mx;
+    }
+    mq[q - 1] = mx;
+  }
+  const double e1 = __longlong_as_double((long long)mq[0]), e2 = __longlong_as_double((long long)mq[1]),
+               e3 = __longlong_as_double((long long)mq[2]);
+  unsigned long long mmax = mq[0] > mq[1] ? mq[0] : mq[1];
+  mmax = mq[2] > mmax ? mq[2] : mmax;
+  const double emax = __longlong_as_double((long long)mmax);
+  const bool ladder = PG_SETSUM_MUL(5.0, e1) <= e2 && PG_SETSUM_MUL(5.0, e2) <= e3;
+  *est = PG_SETSUM_MUL(vol, s5[0]);
+  *err = PG_SETSUM_MUL(vol, ladder ? e1 : PG_SETSUM_MUL(5.0, emax));
+  *bisect = cand >= 0 ? cand : maxdim;
+}
+
+// Widest axis (first strictly widest; a negative or NaN side never wins) and
+// the volume as the product of the sides in axis order (Phases.cuh:329-348).
+__device__ __forceinline__ void side_step(int k, double side, double& vol, unsigned long long& widest, int& maxdim) {
+  const unsigned long long sb = (unsigned long long)__double_as_longlong(side);
+  const unsigned long long key = ((sb >> 63) || (sb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) ? 0ull : sb;
+  if (key > widest) {
+    widest = key;
+    maxdim = k;
+  }
+  vol = (k == 0) ? side : PG_SETSUM_MUL(vol, side);
+}
+
+// Regions [0, n) of a run that starts at list position `base`, one per
+// thread, blocks in list order.  (A grid-stride loop over tens of millions of
+// regions lets the blocks drift apart over the list, and the scattered loads
+// of the SoA rows made each region up to 40% dearer.)  With `segs` (the
+// integrals' segments of the list), a region in the first half of a segment
+// that has a parent level is evaluated together with its sibling in the
+// second half, and second-half regions are left to their sibling's thread;
+// without, every region is evaluated alone.
 template <int MAXD>
 static __global__ void __launch_bounds__(kSetSumThreads, 4)
     setsum_kernel(const double* __restrict__ left, const double* __restrict__ length, uint64_t n, uint64_t stride,
                   const uint32_t* __restrict__ owner, const IntegralDesc* __restrict__ descs, RuleDev rule,
-                  double* __restrict__ est, double* __restrict__ err, int32_t* __restrict__ bisect) {
+                  double* __restrict__ est, double* __restrict__ err, int32_t* __restrict__ bisect,
+                  const SegDesc* __restrict__ segs, uint64_t base) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SetSumSmem<MAXD>& S = *reinterpret_cast<SetSumSmem<MAXD>*>(smem_raw);
+  SetSumSmem<MAXD>& Sm = *reinterpret_cast<SetSumSmem<MAXD>*>(smem_raw);
+  constexpr int T = kSetSumThreads;
+  const uint64_t r = (uint64_t)blockIdx.x * T + threadIdx.x;
+  bool work = r < n;
+  uint32_t j = 0;
+  uint64_t rb = r;  // the sibling evaluated with r (r itself: none)
+  if (work) {
+    j = owner ? owner[r] : 0u;
+    if (segs) {
+      const SegDesc& S = segs[j];
+      const uint64_t local = base + r - S.start, half = S.n / 2;
+      if (S.has_parent && (S.n & 1ull) == 0ull && half > 0) {
+        if (local >= half) work = false;  // evaluated with its sibling
+        rb = r + half;
+        if (rb >= n) rb = r;  // a segment always lies inside one run; never read outside it
+      }
+    }
+  }
+  if (!__syncthreads_or(work)) return;
   for (int q = threadIdx.x; q < (MAXD + 1) * 45; q += kSetSumThreads) {
-    S.w[q] = rule.w[q];
-    S.scale[q] = rule.scale[q];
-    S.norm[q] = rule.norm[q];
+    Sm.w[q] = rule.w[q];
+    Sm.scale[q] = rule.scale[q];
+    Sm.norm[q] = rule.norm[q];
   }
   __syncthreads();
-  double* const fv = S.fd + threadIdx.x;
-  constexpr int T = kSetSumThreads;
-
-  for (uint64_t r = (uint64_t)blockIdx.x * T + threadIdx.x; r < n; r += (uint64_t)gridDim.x * T) {
-    const uint32_t j = owner ? owner[r] : 0u;
-    const IntegralDesc& D = descs[j];
-    const int d = D.d;
-    const bool unit = D.unit != 0;
-    double e0 = 1.0, a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, b = 0.0, g = 0.0, t3 = 0.0, z = 1.0;
-    double vol = 1.0;
-    unsigned long long widest = 0ull;
-    int maxdim = 0;
-    for (int k = 0; k < d; ++k) {
-      const double lo = left[(uint64_t)k * stride + r];
-      const double up = __dadd_rn(lo, length[(uint64_t)k * stride + r]);
-      // Side length, widest axis (first strictly widest, a negative or NaN
-      // side never wins) and the volume as the product of the sides in axis
-      // order (Phases.cuh:329-348).
-      const double side = __dsub_rn(up, lo);
-      const unsigned long long sb = (unsigned long long)__double_as_longlong(side);
-      const unsigned long long sk = ((sb >> 63) || (sb & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) ? 0ull : sb;
-      if (sk > widest) {
-        widest = sk;
-        maxdim = k;
-      }
-      vol = (k == 0) ? side : mul_rn_int(vol, side);
-      // The axis's 11 coordinates (Sample.cuh:126-131) and factors.
-      double h[kCodesPerDim];
-#pragma unroll
-      for (int c = 0; c < kCodesPerDim; ++c) {
-        const double t = __fma_rn(rule.A[c], lo, mul_rn_int(rule.B[c], up));
-        h[c] = family_factor(D, k, unit ? t : __fma_rn(t, D.range[k], D.glo[k]));
-      }
-      fv[(k * kFdValues + 0) * T] = h[0];
-      fv[(k * kFdValues + 1) * T] = h[1];
-      fv[(k * kFdValues + 2) * T] = h[6];
-      fv[(k * kFdValues + 3) * T] = h[2];
-      fv[(k * kFdValues + 4) * T] = h[7];
-      const double c = h[0];
-      const double p0 = __dadd_rn(h[1], h[6]), p1 = __dadd_rn(h[2], h[7]), p2 = __dadd_rn(h[3], h[8]),
-                   p3 = __dadd_rn(h[4], h[9]), p4 = __dadd_rn(h[5], h[10]);
-      t3 = __fma_rn(b, p0, mul_rn_int(t3, c));
-      g = __fma_rn(a1, p0, __fma_rn(a0, p1, mul_rn_int(g, c)));
-      b = __fma_rn(a0, p0, mul_rn_int(b, c));
-      a0 = __fma_rn(e0, p0, mul_rn_int(a0, c));
-      a1 = __fma_rn(e0, p1, mul_rn_int(a1, c));
-      a2 = __fma_rn(e0, p2, mul_rn_int(a2, c));
-      a3 = __fma_rn(e0, p3, mul_rn_int(a3, c));
-      e0 = mul_rn_int(e0, c);
-      z = mul_rn_int(z, p4);
-    }
-    const double jac = D.jac;
-    const bool scale_jac = jac != 1.0;
-
-    // Rule sums: sum_s w[s][r] * S_s, times the box's Jacobian.
-    const double* W = S.w + d * 45;
-    double s5[kNRules];
-#pragma unroll
-    for (int q = 0; q < kNRules; ++q) {
-      double v = mul_rn_int(W[q], e0);
-      v = __fma_rn(W[5 + q], a0, v);
-      v = __fma_rn(W[10 + q], a1, v);
-      v = __fma_rn(W[15 + q], a2, v);
-      v = __fma_rn(W[20 + q], a3, v);
-      v = __fma_rn(W[25 + q], b, v);
-      v = __fma_rn(W[30 + q], g, v);
-      v = __fma_rn(W[35 + q], t3, v);
-      v = __fma_rn(W[40 + q], z, v);
-      s5[q] = scale_jac ? mul_rn_int(v, jac) : v;
-    }
-
-    // Point values of the fourth differences, formed as the point-by-point
-    // evaluation forms them: L * R from the two half products in axis order.
-    const int m = d / 2;
-    double Lc = fv[0], Rc = fv[(m * kFdValues) * T];
-    for (int k = 1; k < m; ++k) Lc = mul_rn_int(Lc, fv[(k * kFdValues) * T]);
-    for (int k = m + 1; k < d; ++k) Rc = mul_rn_int(Rc, fv[(k * kFdValues) * T]);
-    double f0 = mul_rn_int(Lc, Rc);
-    if (scale_jac) f0 = mul_rn_int(f0, jac);
-    const double f02 = __dadd_rn(f0, f0);
-    unsigned long long kmax = 0ull;
-    int cand = -1;
-    double pre = 1.0;  // product of the centre factors of the earlier axes of the current half
-    for (int k = 0; k < d; ++k) {
-      const bool lhalf = k < m;
-      const int hbeg = lhalf ? 0 : m, hend = lhalf ? m : d;
-      double f[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const double hv = fv[(k * kFdValues + 1 + v) * T];
-        double P = (k == hbeg) ? hv : mul_rn_int(pre, hv);
-        for (int q = k + 1; q < hend; ++q) P = mul_rn_int(P, fv[(q * kFdValues) * T]);
-        double fp = lhalf ? mul_rn_int(P, Rc) : mul_rn_int(Lc, P);
-        f[v] = scale_jac ? mul_rn_int(fp, jac) : fp;
-      }
-      const double ck = fv[(k * kFdValues) * T];
-      pre = (k == hbeg) ? ck : mul_rn_int(pre, ck);
-      if (k + 1 == m) pre = 1.0;
-      // base + ratio*(fp+fm) - (fp2+fm2), base = 2*f0*(1-ratio): the
-      // reference's compiled code fuses the base multiply for d <= 4 and the
-      // ratio multiply for d >= 5 (Sample.cuh:190-215).
-      const double X = __dadd_rn(f[0], f[1]);
-      const double Y = __dadd_rn(f[2], f[3]);
-      const double s = (d <= 4) ? __fma_rn(f02, rule.omr, __dmul_rn(rule.ratio, X))
-                                : __fma_rn(rule.ratio, X, __dmul_rn(f02, rule.omr));
-      const unsigned long long fd = (unsigned long long)__double_as_longlong(fabs(__dsub_rn(s, Y)));
-      if (fd != 0ull && fd <= 0x7ff0000000000000ull && fd > kmax) {
-        kmax = fd;
-        cand = k;
-      }
-    }
-
-    // Null-rule error (Sample.cuh:261-289): maxima of non-negative terms on
-    // their bit patterns, a NaN term ignored.
-    const double* SC = S.scale + d * 45;
-    const double* NM = S.norm + d * 45;
-    unsigned long long mq[3] = {0ull, 0ull, 0ull};
-#pragma unroll
-    for (int q = 1; q <= 3; ++q) {
-      unsigned long long mx = 0ull;
-#pragma unroll
-      for (int st = 0; st < kNSets; ++st) {
-        const unsigned long long bt = (unsigned long long)__double_as_longlong(
-            mul_rn_int(fabs(__fma_rn(SC[st * kNRules + q], s5[q], s5[q + 1])), NM[st * kNRules + q]));
-        const unsigned long long term = (bt & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : bt;
-        mx = term > mx ? term : mx;
-      }
-      mq[q - 1] = mx;
-    }
-    const double e1 = __longlong_as_double((long long)mq[0]), e2 = __longlong_as_double((long long)mq[1]),
-                 e3 = __longlong_as_double((long long)mq[2]);
-    unsigned long long mmax = mq[0] > mq[1] ? mq[0] : mq[1];
-    mmax = mq[2] > mmax ? mq[2] : mmax;
-    const double emax = __longlong_as_double((long long)mmax);
-    const bool ladder = mul_rn_int(5.0, e1) <= e2 && mul_rn_int(5.0, e2) <= e3;
-    est[r] = mul_rn_int(vol, s5[0]);
-    err[r] = mul_rn_int(vol, ladder ? e1 : mul_rn_int(5.0, emax));
-    bisect[r] = cand >= 0 ? cand : maxdim;
+  double* const fv = Sm.fd + threadIdx.x;
+  double* const fvb = Sm.fd + (MAXD * kFdValues) * T + threadIdx.x;
+  if (!work) return;
+  const bool pair = rb != r;
+  const IntegralDesc& D = descs[j];
+  const int d = D.d;
+  const bool unit = D.unit != 0;
+  // The deferred axis: the one the siblings differ on, else the last.
+  int s = d - 1;
+  if (pair)
+    for (int k = d - 1; k >= 0; --k)
+      if (left[(uint64_t)k * stride + r] != left[(uint64_t)k * stride + rb]) s = k;
+  SetSums Q{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0};
+  AxisTerm As{};
+  double vol = 1.0, volb = 1.0;
+  unsigned long long widest = 0ull, widestb = 0ull;
+  int maxdim = 0, maxdimb = 0;
+  // The sibling's own side and factors on the deferred axis.
+  double sideb = 0.0;
+  AxisTerm Bs{};
+  if (pair) {
+    const double lo = left[(uint64_t)s * stride + rb];
+    const double up = __dadd_rn(lo, length[(uint64_t)s * stride + rb]);
+    sideb = __dsub_rn(up, lo);
+    Bs = axis_term(D, rule, s, lo, up, unit, fvb, T);
+  }
+  for (int k = 0; k < d; ++k) {
+    const double lo = left[(uint64_t)k * stride + r];
+    const double up = __dadd_rn(lo, length[(uint64_t)k * stride + r]);
+    const double side = __dsub_rn(up, lo);
+    side_step(k, side, vol, widest, maxdim);
+    if (pair) side_step(k, k == s ? sideb : side, volb, widestb, maxdimb);
+    const AxisTerm A = axis_term(D, rule, k, lo, up, unit, fv + (k * kFdValues) * T, T);
+    if (k == s)
+      As = A;
+    else
+      set_step(Q, A);
+  }
+  const double jac = D.jac;
+  {
+    SetSums R = Q;
+    set_step(R, As);
+    region_result<MAXD>(Sm, rule, R, d, jac, vol, maxdim, fv, -1, fv, &est[r], &err[r], &bisect[r]);
+  }
+  if (pair) {
+    SetSums R = Q;
+    set_step(R, Bs);
+    region_result<MAXD>(Sm, rule, R, d, jac, volb, maxdimb, fv, s, fvb, &est[rb], &err[rb], &bisect[rb]);
   }
 }
 
-// Launch of the set-sum kernel over a region list whose integrals all have
-// product-form families: a grid-stride loop with at most 8 blocks per SM.
+// Launch of the set-sum kernel over a run of the region list whose integrals
+// all have product-form families: one thread per region.  `segs` may be null
+// (no sibling pairing); `base` is the run's first list position.
 template <int MAXD>
-inline cudaError_t launch_setsum_shape(const pg_eval_args& a) {
+inline cudaError_t launch_setsum_shape(const pg_eval_args& a, const SegDesc* segs, uint64_t base) {
   const size_t smem = sizeof(SetSumSmem<MAXD>);
   static std::atomic<unsigned long long> attr_done{0};
   const cudaError_t ae = ensure_dynamic_smem(setsum_kernel<MAXD>, (int)smem, attr_done);
   if (ae != cudaSuccess) return ae;
-  const uint64_t want = (a.n + kSetSumThreads - 1) / kSetSumThreads;
-  const uint64_t cap = (uint64_t)(a.num_sms > 0 ? a.num_sms : 1) * 8ull;
-  const uint64_t g = want < cap ? want : cap;
-  setsum_kernel<MAXD><<<(unsigned)(g > 0 ? g : 1), kSetSumThreads, smem, (cudaStream_t)a.stream>>>(
+  if (a.n == 0) return cudaSuccess;
+  const uint64_t g = (a.n + kSetSumThreads - 1) / kSetSumThreads;
+  if (g > 0x7fffffffull) return cudaErrorInvalidValue;
+  setsum_kernel<MAXD><<<(unsigned)g, kSetSumThreads, smem, (cudaStream_t)a.stream>>>(
       a.left, a.length, a.n, a.stride, a.owner, static_cast<const IntegralDesc*>(a.descs),
-      *static_cast<const RuleDev*>(a.rule), a.est, a.err, a.bisect);
+      *static_cast<const RuleDev*>(a.rule), a.est, a.err, a.bisect, segs, base);
   return cudaGetLastError();
 }
 
-inline cudaError_t launch_setsum(const pg_eval_args& a) {
-  return a.maxd <= 8 ? launch_setsum_shape<8>(a) : launch_setsum_shape<kMaxNdim>(a);
+inline cudaError_t launch_setsum(const pg_eval_args& a, const SegDesc* segs, uint64_t base) {
+  return a.maxd <= 8 ? launch_setsum_shape<8>(a, segs, base) : launch_setsum_shape<kMaxNdim>(a, segs, base);
 }
 
 }  // namespace pg

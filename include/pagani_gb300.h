@@ -151,6 +151,19 @@ typedef struct pg_stats {
   uint64_t setsum_regions;      /* regions evaluated by generator-set sums (PG_EVAL_SET_SUMS) */
 } pg_stats;
 
+/* One iteration of a run (recorded while profiling is on): regions in the
+ * list, integrals resident, evaluation launches and their CUDA-event time, and
+ * the time of the two-level/classification launches.  No counterpart in the
+ * reference, whose debug mode writes per-iteration CSV files instead
+ * (cuda/pagani/quad/GPUquad/PaganiUtils.cuh:203-241). */
+typedef struct pg_iteration_record {
+  uint64_t regions;
+  uint32_t integrals;
+  uint32_t eval_launches;
+  double eval_ms;
+  double stage_ms;
+} pg_iteration_record;
+
 void pg_options_default(pg_options* opt);
 int pg_feval(int ndim); /* points per region: cuda/pagani/quad/quad.h:67-76 */
 
@@ -162,6 +175,9 @@ const char* pg_last_error(const pg_context* ctx);
 int pg_context_set_profiling(pg_context* ctx, int on);
 int pg_context_stats(const pg_context* ctx, pg_stats* out);
 int pg_context_reset_stats(pg_context* ctx);
+/* The iterations recorded since the last pg_context_reset_stats: *count
+ * receives their number, out[0 .. min(count, capacity)) the records. */
+int pg_context_iterations(const pg_context* ctx, pg_iteration_record* out, uint64_t capacity, uint64_t* count);
 void* pg_context_stream(pg_context* ctx); /* the cudaStream_t the context launches on */
 int pg_synchronize(pg_context* ctx);
 

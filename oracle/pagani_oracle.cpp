@@ -521,8 +521,12 @@ static bool product_form(int family) {
          family == FAM_PRODUCT;
 }
 
+// The recurrence takes the axes other than `defer` in axis order, then
+// `defer` (the library evaluates two siblings together and defers the axis
+// they differ on; a region evaluated alone defers its last axis, which is the
+// plain axis order).
 static EvalOut eval_region_setsums(const Rule& R, const Prepared& P, const double* lows, const double* highs,
-                                   const double* lower, const double* length) {
+                                   const double* lower, const double* length, int defer) {
   const int d = R.ndim;
   double jac = 1.0;
   for (int k = 0; k < d; ++k) jac = jac * (highs[k] - lows[k]);
@@ -539,7 +543,23 @@ static EvalOut eval_region_setsums(const Rule& R, const Prepared& P, const doubl
   double vol = 1.0, widest = 0.0;
   int maxdim = 0;
   double fv[kMaxDim][5];  // centre, +G0, -G0, +G1, -G1
-  for (int k = 0; k < d; ++k) {
+  double pd[6] = {0, 0, 0, 0, 0, 0};  // c, p0..p4 of the deferred axis
+  for (int kk = 0; kk <= d; ++kk) {
+    // kk < d: axis kk (the deferred one only stores its terms); kk == d: the deferred axis enters
+    const int k = kk == d ? defer : kk;
+    if (kk == d) {
+      const double c = pd[0], p0 = pd[1], p1 = pd[2], p2 = pd[3], p3 = pd[4], p4 = pd[5];
+      t3 = std::fma(b, p0, t3 * c);
+      g = std::fma(a1, p0, std::fma(a0, p1, g * c));
+      b = std::fma(a0, p0, b * c);
+      a0 = std::fma(e0, p0, a0 * c);
+      a1 = std::fma(e0, p1, a1 * c);
+      a2 = std::fma(e0, p2, a2 * c);
+      a3 = std::fma(e0, p3, a3 * c);
+      e0 = e0 * c;
+      z = z * p4;
+      break;
+    }
     const double lo = lower[k], up = lo + length[k];
     const double side = up - lo;
     if (side > widest) {
@@ -561,6 +581,10 @@ static EvalOut eval_region_setsums(const Rule& R, const Prepared& P, const doubl
     fv[k][4] = h[7];
     const double c = h[0];
     const double p0 = h[1] + h[6], p1 = h[2] + h[7], p2 = h[3] + h[8], p3 = h[4] + h[9], p4 = h[5] + h[10];
+    if (k == defer) {
+      pd[0] = c, pd[1] = p0, pd[2] = p1, pd[3] = p2, pd[4] = p3, pd[5] = p4;
+      continue;
+    }
     t3 = std::fma(b, p0, t3 * c);
     g = std::fma(a1, p0, std::fma(a0, p1, g * c));
     b = std::fma(a0, p0, b * c);
@@ -647,10 +671,14 @@ static void parallel_for(size_t n, int nthreads, const std::function<void(size_t
   for (auto& t : th) t.join();
 }
 
+// With `siblings`, regions i and i + n/2 (n even) are the two children of one
+// region (the list layout after a split): the set-sum evaluation defers the
+// axis they differ on, as the library does when it evaluates them together.
 static void evaluate_all(const Rule& R, const Prepared& P, const double* lows, const double* highs, size_t n,
                          const double* left, const double* len, double* est, double* err, int32_t* bis,
-                         int nthreads) {
+                         int nthreads, bool siblings = false) {
   const int d = R.ndim;
+  const bool pairs = siblings && n % 2 == 0 && n > 0;
   parallel_for(n, nthreads, [&](size_t b, size_t e) {
     double lo[kMaxDim], ln[kMaxDim];
     for (size_t i = b; i < e; ++i) {
@@ -658,8 +686,15 @@ static void evaluate_all(const Rule& R, const Prepared& P, const double* lows, c
         lo[k] = left[(size_t)k * n + i];
         ln[k] = len[(size_t)k * n + i];
       }
-      const EvalOut o = (g_eval_mode == 1 && product_form(P.family)) ? eval_region_setsums(R, P, lows, highs, lo, ln)
-                                                                     : eval_region(R, P, lows, highs, lo, ln);
+      int defer = d - 1;
+      if (pairs) {
+        const size_t j = i < n / 2 ? i + n / 2 : i - n / 2;
+        for (int k = d - 1; k >= 0; --k)
+          if (left[(size_t)k * n + i] != left[(size_t)k * n + j]) defer = k;
+      }
+      const EvalOut o = (g_eval_mode == 1 && product_form(P.family))
+                            ? eval_region_setsums(R, P, lows, highs, lo, ln, defer)
+                            : eval_region(R, P, lows, highs, lo, ln);
       est[i] = o.est;
       err[i] = o.err;
       bis[i] = o.bisect;
@@ -1004,7 +1039,8 @@ int orc_integrate_regions(const orc::Integrand* f, double epsrel, double epsabs,
     err.assign(n, 0);
     bis.assign(n, 0);
     act.assign(n, 1);
-    evaluate_all(R, P, lows, highs, n, left.data(), len.data(), est.data(), err.data(), bis.data(), nthreads);
+    evaluate_all(R, P, lows, highs, n, left.data(), len.data(), est.data(), err.data(), bis.data(), nthreads,
+                 have_parent);
     cum.neval += n * fev;
     const double iter_est = canon_sum(n, [&](size_t i) { return est[i]; });
     const bool relerr =

@@ -15,6 +15,7 @@ MIRRORS = {
     "pg_options": pg.PgOptions,
     "pg_stats": pg.PgStats,
     "pg_mcubes_options": pg.PgMcubesOptions,
+    "pg_iteration_record": pg.PgIterationRecord,
 }
 
 
