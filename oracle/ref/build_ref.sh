@@ -21,4 +21,9 @@ if [ -f "$HERE/ref_phase1.cu" ]; then
   $NVCC -std=c++17 --expt-relaxed-constexpr -w -I"$REF" -I"$REF/externals" -I"$HERE/../.." \
     -gencode arch=compute_103a,code=sm_103a -cubin -o "$OUT/ref_phase1.cubin" "$HERE/ref_phase1.cu"
 fi
+# Reference two-level, filter and split kernels as a cubin (same loading path).
+if [ -f "$HERE/ref_stages.cu" ]; then
+  $NVCC -std=c++17 --expt-relaxed-constexpr -w -I"$REF" -I"$REF/externals" \
+    -gencode arch=compute_103a,code=sm_103a -cubin -o "$OUT/ref_stages.cubin" "$HERE/ref_stages.cu"
+fi
 echo "build_ref: done -> $OUT"
