@@ -46,6 +46,7 @@ def load():
     lib.orc_feval.restype = ctypes.c_int
     lib.orc_set_eval_mode.argtypes = [ctypes.c_int]
     lib.orc_set_eval_mode.restype = ctypes.c_int
+    lib.orc_budget_fixes.restype = ctypes.c_int
     lib.orc_rule_tables.argtypes = [ctypes.c_int, _D, _D, _D, P(ctypes.c_int32), _D]
     lib.orc_eval_point.restype = ctypes.c_double
     lib.orc_eval_point.argtypes = [vp, _D]
@@ -115,6 +116,11 @@ class eval_mode:
 
     def __exit__(self, *a):
         load().orc_set_eval_mode(0)
+
+
+def budget_fixes():
+    """Iterations of the last integration in which fix_error_budget_overflow fired."""
+    return load().orc_budget_fixes()
 
 
 def evaluate_regions(f, left, length, lows=None, highs=None, nthreads=None):

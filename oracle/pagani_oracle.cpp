@@ -655,6 +655,8 @@ static EvalOut eval_region_setsums(const Rule& R, const Prepared& P, const doubl
 // Evaluation mode of the oracle's evaluate_all: 0 point by point (the
 // reference's order), 1 generator-set sums for the product-form families.
 static int g_eval_mode = 0;
+// Iterations of the last integration in which fix_error_budget_overflow fired.
+static int g_budget_fixes = 0;
 
 static void parallel_for(size_t n, int nthreads, const std::function<void(size_t, size_t)>& body) {
   if (nthreads <= 1 || n < 64) {
@@ -888,6 +890,8 @@ int orc_feval(int ndim) { return orc::feval_count(ndim); }
 
 // Region-evaluation mode of every later evaluation and integration call:
 // 0 point by point, 1 generator-set sums for the product-form families.
+int orc_budget_fixes(void) { return orc::g_budget_fixes; }
+
 int orc_set_eval_mode(int mode) {
   if (mode != 0 && mode != 1) return -1;
   orc::g_eval_mode = mode;
@@ -1002,6 +1006,7 @@ int orc_integrate_regions(const orc::Integrand* f, double epsrel, double epsabs,
   using namespace orc;
   const int d = f->ndim;
   if (d < 2 || d > 15 || !out) return -1;
+  g_budget_fixes = 0;
   const Rule R = make_rule(d);
   const Prepared P = prepare(*f);
   const int parts = d < 5 ? 4 : (d <= 10 ? 2 : 1);
@@ -1087,6 +1092,7 @@ int orc_integrate_regions(const orc::Integrand* f, double epsrel, double epsabs,
       const double leaves_est = cum.estimate + iter_est;
       const double leaves_fin_err = cum.errorest + fin_err;
       if (leaves_fin_err > std::fabs(leaves_est) * epsrel) {
+        ++g_budget_fixes;
         std::fill(act.begin(), act.end(), 1);
         fin_err = 0.;
         fin_est = 0.;

@@ -111,6 +111,8 @@ def test_oracle_full_loop_matches_reference_run(orc, case):
     name, f, eps, _ = case
     r, _ = orc.integrate(f, eps, 0.0)
     _check_result(name, r)
+    # fix_error_budget_overflow (Workspace.cuh:121-146) fires in as many iterations as in the reference's run
+    assert orc.budget_fixes() == int(GOLD[f"{name}/fixed"].sum())
 
 
 @needs_gold
