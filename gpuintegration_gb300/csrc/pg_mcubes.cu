@@ -6,15 +6,19 @@
 //     axis, ncubes = ng^d, npg = max(ncall/ncubes, 2) samples per cube, 500 bins
 //     per axis, the same point map, weights and per-cube variance term;
 //   * random numbers from Philox4x32-10 (Salmon et al., SC'11), keyed by the
-//     seed with counter (cube, sample, axis pair, iteration), so a run is
-//     reproducible from its seed (the reference seeds XORWOW from the clock,
-//     vegasT.cuh:801-803);
-//   * per-bin sums of f^2 in a shared-memory histogram per block, flushed once
-//     per block, instead of one global atomic per sample and axis;
-//   * a fixed grid of 1024 x 256 threads, each taking a contiguous run of cubes,
-//     and block-tree sums: the estimate does not depend on the GPU's SM count;
-//   * grid smoothing and rebinning on the host between iterations, damping
-//     exponent alpha (1.5 in the reference's GPU code, vegas_utils.cuh:139).
+//     seed with counter (cube, sample, axis pair, iteration) (the reference
+//     seeds XORWOW from the clock, vegasT.cuh:801-803);
+//   * per-bin sums of f^2 formed in a fixed order (mcubes_kernel, then
+//     mcubes_bins_kernel over the blocks), and every other sum in a fixed
+//     order too, so a run is reproducible bit for bit from its seed;
+//   * a fixed grid of 1024 x 256 threads: the estimate does not depend on the
+//     GPU's SM count;
+//   * the weighted mean over iterations, the convergence test, the smoothing
+//     of the bin sums and the rebinning with damping exponent alpha (1.5 in the
+//     reference's GPU code, vegas_utils.cuh:139; vegasT.cuh:834-910) run on
+//     the device (mcubes_update_kernel).  The host enqueues every iteration at
+//     once; after convergence the remaining iterations' kernels return at once,
+//     so a run needs one synchronisation instead of one per iteration.
 #include "pg_mcubes.h"
 
 #include "pg_mcubes_kernel.cuh"
@@ -28,7 +32,7 @@ namespace pg {
 
 struct McubesState {
   Engine* eng = nullptr;
-  DevBuf xi, bins, partial;
+  DevBuf xi, bins, part_hist, partial, scratch, state;
 };
 
 McubesState* mcubes_create(Engine* eng) {
@@ -39,17 +43,18 @@ McubesState* mcubes_create(Engine* eng) {
 
 void mcubes_destroy(McubesState* st) {
   if (!st) return;
-  if (st->xi.p) cudaFree(st->xi.p);
-  if (st->bins.p) cudaFree(st->bins.p);
-  if (st->partial.p) cudaFree(st->partial.p);
+  DevBuf* bufs[] = {&st->xi, &st->bins, &st->part_hist, &st->partial, &st->scratch, &st->state};
+  for (DevBuf* b : bufs)
+    if (b->p) cudaFree(b->p);
   delete st;
 }
 
 namespace {
 
 // Rebinning of one axis so every new bin holds the same share of r
-// (vegasT.cuh:616-637).  xi[0..nd] with xi[0] = 0, r[1..nd].
-void rebin(double rc, int nd, const double* r, double* xin, double* xi) {
+// (vegasT.cuh:616-637; Lepage's VEGAS, J. Comput. Phys. 27 (1978) 192).
+// xi[0..nd] with xi[0] = 0, r[1..nd].
+__host__ __device__ void rebin(double rc, int nd, const double* r, double* xin, double* xi) {
   int k = 0;
   double dr = 0.0, xn = 0.0, xo = 0.0;
   for (int i = 1; i < nd; i++) {
@@ -63,10 +68,90 @@ void rebin(double rc, int nd, const double* r, double* xin, double* xi) {
   xi[nd] = 1.0;
 }
 
-int status_of(double est, double err, int it, double epsrel, double epsabs) {
-  // GetStatus (vegas_utils.cuh:237-248)
-  const bool ok = std::fabs(err / est) <= epsrel || err <= epsabs;
-  return (ok && it >= 5) ? 0 : 1;
+// Sum of the blocks' histograms, bin by bin, in block order.
+__global__ void mcubes_bins_kernel(const double* __restrict__ part_hist, int nbins_total, double* __restrict__ bins,
+                                   const McState* __restrict__ state) {
+  if (state->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbins_total) return;
+  double s = 0.0;
+  for (int b = 0; b < kMcBlocks; ++b) s = s + part_hist[(size_t)b * nbins_total + i];
+  bins[i] = s;
+}
+
+struct McUpdate {
+  int it, adapt, skip, d, nd;
+  double epsrel, epsabs, dv2g, xnd, alpha;
+};
+
+// One iteration's bookkeeping (vegasT.cuh:834-910): the iteration's estimate
+// and variance from the block sums, the weighted mean, chi^2 and status, then
+// (adapting iterations) per axis the smoothing of the bin sums and the
+// rebinning.  One warp per axis.  `bins` is smoothed in place; scratch holds
+// r and xin per axis.
+__global__ void mcubes_update_kernel(McUpdate U, const double* __restrict__ partial, double* __restrict__ bins,
+                                     double* __restrict__ xi, double* __restrict__ scratch, McState* state) {
+  __shared__ int go;
+  if (threadIdx.x == 0) go = state->stop == 0;
+  __syncthreads();
+  if (!go) return;
+  const int nb1 = U.nd + 1;
+  if (threadIdx.x == 0) {
+    double ti = 0.0, tsi = 0.0;
+    for (int b = 0; b < kMcBlocks; ++b) {
+      ti = ti + partial[2 * b];
+      tsi = tsi + partial[2 * b + 1];
+    }
+    tsi = tsi * U.dv2g;
+    McState S = *state;
+    if (!U.adapt || U.it > U.skip) {
+      const double wgt = 1.0 / tsi;
+      S.si = S.si + wgt * ti;
+      S.schi = S.schi + wgt * ti * ti;
+      S.swgt = S.swgt + wgt;
+      S.tgral = S.si / S.swgt;
+      S.chi2a = (S.schi - S.si * S.tgral) / (static_cast<double>(U.it) - 0.9999);
+      if (S.chi2a < 0.0) S.chi2a = 0.0;
+      S.sd = sqrt(1.0 / S.swgt);
+      // GetStatus (vegas_utils.cuh:237-248)
+      const bool ok = fabs(S.sd / S.tgral) <= U.epsrel || S.sd <= U.epsabs;
+      S.status = (ok && U.it >= 5) ? 0 : 1;
+    }
+    S.iters += 1;
+    S.stop = S.status == 0;
+    *state = S;
+  }
+  if (!U.adapt) return;
+  const int j = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (j >= U.d) return;
+  double* dj = bins + (size_t)j * nb1;
+  double* r = scratch + (size_t)j * 2 * nb1;
+  double* xin = r + nb1;
+  __shared__ double dt[kMaxDim];
+  if (lane == 0) {
+    double xo = dj[1], xn = dj[2];
+    dj[1] = (xo + xn) / 2.0;
+    double t = dj[1];
+    for (int i = 2; i < U.nd; ++i) {
+      const double rcv = xo + xn;
+      xo = xn;
+      xn = dj[i + 1];
+      dj[i] = (rcv + xn) / 3.0;
+      t = t + dj[i];
+    }
+    dj[U.nd] = (xo + xn) / 2.0;
+    dt[j] = t + dj[U.nd];
+  }
+  __syncwarp();
+  const double dtj = dt[j];
+  if (!(dtj > 0.0)) return;  // no contribution on this axis: the grid stays
+  for (int i = 1 + lane; i <= U.nd; i += 32) r[i] = pow((1.0 - dj[i] / dtj) / (log(dtj) - log(dj[i])), U.alpha);
+  __syncwarp();
+  if (lane == 0) {
+    double rsum = 0.0;
+    for (int i = 1; i <= U.nd; ++i) rsum = rsum + r[i];
+    rebin(rsum / U.xnd, U.nd, r, xin, xi + (size_t)j * nb1);
+  }
 }
 
 }  // namespace
@@ -82,6 +167,10 @@ int mcubes_run(McubesState* st, const IntegralDesc& D, double epsrel, double eps
   const int nd = opt.nbins > 1 ? opt.nbins : 500;
   if (opt.ncall < 2 || opt.titer < 1 || opt.itmax < 0) {
     if (why) *why = "m-Cubes needs ncall >= 2 and titer >= 1";
+    return PG_BAD_ARG;
+  }
+  if (nd > 65535) {
+    if (why) *why = "at most 65535 bins per axis";
     return PG_BAD_ARG;
   }
   // Geometry (vegasT.cuh:704-735).
@@ -110,27 +199,37 @@ int mcubes_run(McubesState* st, const IntegralDesc& D, double epsrel, double eps
     xjac *= dx[j];
   }
   const int nb1 = nd + 1;
-  std::vector<double> xi((size_t)d * nb1, 0.0), r(nb1, 1.0), xin(nb1, 0.0), dbin((size_t)d * nb1, 0.0), dt(d);
+  std::vector<double> xi((size_t)d * nb1, 0.0), r(nb1, 1.0), xin(nb1, 0.0);
   for (int j = 0; j < d; ++j) {
     xi[(size_t)j * nb1 + 1] = 1.0;
     rebin(1.0 / xnd, nd, r.data(), xin.data(), &xi[(size_t)j * nb1]);
   }
-  int rc;
-  if ((rc = E->ensure(st->xi, xi.size() * 8)) != PG_OK || (rc = E->ensure(st->bins, xi.size() * 8)) != PG_OK ||
-      (rc = E->ensure(st->partial, kMcBlocks * 2 * 8)) != PG_OK) {
-    if (why) *why = E->last_error;
-    return rc;
-  }
-  cudaStream_t s = E->stream();
-  const size_t smem = 2 * (size_t)d * nb1 * 8;
-  auto fail = [&](cudaError_t e, const char* what) {
-    if (why) *why = std::string(what) + ": " + cudaGetErrorString(e);
-    return e == cudaErrorMemoryAllocation ? PG_OOM : PG_CUDA_ERROR;
-  };
+  const size_t nbt = (size_t)d * nb1;
+  const size_t smem = mcubes_smem_bytes(d, nd);
   if (smem > kMcMaxSmem) {
     if (why) *why = "too many bins for this dimension";
     return PG_BAD_ARG;
   }
+  int rc;
+  if ((rc = E->ensure(st->xi, nbt * 8)) != PG_OK || (rc = E->ensure(st->bins, nbt * 8)) != PG_OK ||
+      (rc = E->ensure(st->part_hist, (size_t)kMcBlocks * nbt * 8)) != PG_OK ||
+      (rc = E->ensure(st->partial, kMcBlocks * 2 * 8)) != PG_OK ||
+      (rc = E->ensure(st->scratch, 2 * nbt * 8)) != PG_OK || (rc = E->ensure(st->state, sizeof(McState))) != PG_OK) {
+    if (why) *why = E->last_error;
+    return rc;
+  }
+  cudaStream_t s = E->stream();
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (why) *why = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? PG_OOM : PG_CUDA_ERROR;
+  };
+  McState S0;
+  std::memset(&S0, 0, sizeof S0);
+  S0.status = 1;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(st->state.p, &S0, sizeof S0, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(st->xi.p, xi.data(), nbt * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    return fail(e, "m-Cubes setup");
   McArgs A;
   std::memset(&A, 0, sizeof A);
   A.desc = D;
@@ -149,114 +248,59 @@ int mcubes_run(McubesState* st, const IntegralDesc& D, double epsrel, double eps
   A.key0 = (uint32_t)opt.seed;
   A.key1 = (uint32_t)(opt.seed >> 32);
   A.xi = (const double*)st->xi.p;
-  A.bins = (double*)st->bins.p;
+  A.part_hist = (double*)st->part_hist.p;
   A.partial = (double*)st->partial.p;
-  std::vector<double> part(kMcBlocks * 2);
-  double si = 0, swgt = 0, schi = 0, tgral = 0, sd = 0, chi2a = 0;
-  int status = 1;
-  uint64_t iters = 0;
-  auto launch = [&](int it, int adapt) -> int {
+  A.state = (const McState*)st->state.p;
+  McUpdate U;
+  U.skip = opt.skip;
+  U.d = d;
+  U.nd = nd;
+  U.epsrel = epsrel;
+  U.epsabs = epsabs;
+  U.dv2g = dv2g;
+  U.xnd = xnd;
+  U.alpha = opt.alpha;
+  // Every iteration is enqueued at once: the adapting iterations
+  // (vegasT.cuh:784-911), then the frozen-grid ones (vegasT.cuh:921-977);
+  // the kernels of iterations after convergence return at once.
+  for (int it = 1; it <= opt.titer; ++it) {
+    const int adapt = it <= opt.itmax;
     A.iter = (uint32_t)it;
     A.adapt = adapt;
-    cudaError_t e;
-    if ((e = cudaMemcpyAsync(st->xi.p, xi.data(), xi.size() * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-      return fail(e, "grid upload");
-    if (adapt && (e = cudaMemsetAsync(st->bins.p, 0, xi.size() * 8, s)) != cudaSuccess) return fail(e, "memset");
     pg_mcubes_args la;
     la.args = &A;
     la.smem = smem;
     la.stream = (void*)s;
     la.maxd = d;
     la.pad = 0;
-    e = launcher(la);
+    if ((e = launcher(la)) != cudaSuccess) return fail(e, "m-Cubes launch");
     E->stats.launches++;
-    E->stats.points_evaluated += (uint64_t)calls;
-    if (e != cudaSuccess) return fail(e, "m-Cubes launch");
-    if ((e = cudaMemcpyAsync(part.data(), st->partial.p, part.size() * 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return fail(e, "readback");
-    if (adapt &&
-        (e = cudaMemcpyAsync(dbin.data(), st->bins.p, dbin.size() * 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return fail(e, "readback");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail(e, "m-Cubes iteration");
-    return PG_OK;
-  };
-  auto totals = [&](double* ti, double* tsi) {
-    double a = 0, b = 0;
-    for (int bI = 0; bI < kMcBlocks; ++bI) {
-      a += part[2 * bI];
-      b += part[2 * bI + 1];
+    if (adapt) {
+      mcubes_bins_kernel<<<(unsigned)((nbt + 255) / 256), 256, 0, s>>>((const double*)st->part_hist.p, (int)nbt,
+                                                                      (double*)st->bins.p, A.state);
+      E->stats.launches++;
     }
-    *ti = a;
-    *tsi = b * dv2g;
-  };
-  // Adapting iterations (vegasT.cuh:784-911).
-  for (int it = 1; it <= opt.itmax && status == 1; ++iters, ++it) {
-    if ((rc = launch(it, 1)) != PG_OK) return rc;
-    double ti, tsi;
-    totals(&ti, &tsi);
-    if (it > opt.skip) {
-      const double wgt = 1.0 / tsi;
-      si += wgt * ti;
-      schi += wgt * ti * ti;
-      swgt += wgt;
-      tgral = si / swgt;
-      chi2a = (schi - si * tgral) / (static_cast<double>(it) - 0.9999);
-      if (chi2a < 0.0) chi2a = 0.0;
-      sd = std::sqrt(1.0 / swgt);
-      status = status_of(tgral, sd, it, epsrel, epsabs);
-    }
-    // Smooth the bin sums and rebin every axis (vegasT.cuh:873-910).
-    for (int j = 0; j < d; ++j) {
-      double* dj = &dbin[(size_t)j * nb1];
-      double xo = dj[1], xn = dj[2];
-      dj[1] = (xo + xn) / 2.0;
-      dt[j] = dj[1];
-      for (int i = 2; i < nd; ++i) {
-        const double rcv = xo + xn;
-        xo = xn;
-        xn = dj[i + 1];
-        dj[i] = (rcv + xn) / 3.0;
-        dt[j] += dj[i];
-      }
-      dj[nd] = (xo + xn) / 2.0;
-      dt[j] += dj[nd];
-    }
-    for (int j = 0; j < d; ++j) {
-      if (dt[j] > 0.0) {
-        const double* dj = &dbin[(size_t)j * nb1];
-        double rsum = 0.0;
-        for (int i = 1; i <= nd; ++i) {
-          r[i] = std::pow((1.0 - dj[i] / dt[j]) / (std::log(dt[j]) - std::log(dj[i])), opt.alpha);
-          rsum += r[i];
-        }
-        rebin(rsum / xnd, nd, r.data(), xin.data(), &xi[(size_t)j * nb1]);
-      }
-    }
+    U.it = it;
+    U.adapt = adapt;
+    mcubes_update_kernel<<<1, 32 * d, 0, s>>>(U, (const double*)st->partial.p, (double*)st->bins.p,
+                                              (double*)st->xi.p, (double*)st->scratch.p, (McState*)st->state.p);
+    E->stats.launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "m-Cubes launch");
   }
-  // Frozen-grid iterations (vegasT.cuh:921-977).
-  for (int it = opt.itmax + 1; it <= opt.titer && status; ++iters, ++it) {
-    if ((rc = launch(it, 0)) != PG_OK) return rc;
-    double ti, tsi;
-    totals(&ti, &tsi);
-    const double wgt = 1.0 / tsi;
-    si += wgt * ti;
-    schi += wgt * ti * ti;
-    swgt += wgt;
-    tgral = si / swgt;
-    chi2a = (schi - si * tgral) / (it - 0.9999);
-    if (chi2a < 0.0) chi2a = 0.0;
-    sd = std::sqrt(1.0 / swgt);
-    status = status_of(tgral, sd, it, epsrel, epsabs);
-  }
+  McState S;
+  if ((e = cudaMemcpyAsync(&S, st->state.p, sizeof S, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail(e, "m-Cubes run");
+  E->stats.points_evaluated += (uint64_t)calls * S.iters;
   pg_result R;
   std::memset(&R, 0, sizeof R);
-  R.estimate = tgral;
-  R.errorest = sd;
-  R.chi_sq = chi2a;
-  R.neval = (uint64_t)calls * iters;
+  R.estimate = S.tgral;
+  R.errorest = S.sd;
+  R.chi_sq = S.chi2a;
+  R.neval = (uint64_t)calls * S.iters;
   R.nregions = (uint64_t)ncubes;
-  R.iters = iters;
-  R.status = status;
+  R.iters = S.iters;
+  R.status = S.status;
   R.last_phase = -1;
   *out = R;
   return PG_OK;

@@ -6,8 +6,16 @@
 //   * the same point map, weights and per-cube variance term;
 //   * random numbers from Philox4x32-10 (Salmon et al., SC'11), keyed by the
 //     seed with counter (cube, sample, axis pair, iteration);
-//   * per-bin sums of f^2 in a shared-memory histogram per block, flushed once
-//     per block, instead of one global atomic per sample and axis;
+//   * per-bin sums of f^2 accumulated in a fixed order, so a seed reproduces
+//     a run bit for bit: the reference adds every sample to every axis's bin
+//     with a global floating-point atomic (vegasT.cuh:304-307), whose order
+//     varies from run to run.  Here each block samples in rounds, one sample
+//     per thread; after a round warp w adds the round's samples to the bins
+//     of axis w (and w + 8), 32 samples at a time: samples that fall into one
+//     bin are summed by the lowest lane among them in lane order
+//     (__match_any_sync), and that lane adds the sum to the block's
+//     shared-memory histogram.  Blocks write their histograms to global
+//     memory, and mcubes_bins_kernel sums them over the blocks in block order;
 //   * a fixed grid of 1024 x 256 threads, each taking a contiguous run of
 //     cubes, and block-tree sums, so the estimate does not depend on the SM count.
 // Every floating-point operation is an explicit IEEE intrinsic.
@@ -47,6 +55,15 @@ __host__ __device__ __forceinline__ double philox_unit(uint32_t a, uint32_t b) {
   return (double)(m + 1) * 1.1102230246251565404236316680908203125e-16;  // 2^-53
 }
 
+// Device-side state of one m-Cubes run (the weighted mean over iterations,
+// vegasT.cuh:834-852, and the stop flag of the iteration loop).
+struct McState {
+  double si, schi, swgt, tgral, sd, chi2a;
+  int32_t status;  // 1 until the result meets the tolerance (GetStatus, vegas_utils.cuh:237-248)
+  int32_t stop;    // nonzero: the loop has ended, later iterations' kernels return at once
+  uint64_t iters;
+};
+
 struct McArgs {
   IntegralDesc desc;
   int d, ng, npg, nbins;
@@ -56,42 +73,62 @@ struct McArgs {
   uint32_t key0, key1, iter;
   int adapt;
   const double* xi;   // [d][nbins + 1], xi[j][0] = 0
-  double* bins;       // [d][nbins + 1] sums of f^2 per bin (adapt)
-  double* partial;    // [kMcBlocks][2]
+  double* part_hist;  // [kMcBlocks][d * (nbins + 1)] per-block sums of f^2 per bin (adapt)
+  double* partial;    // [kMcBlocks][2] per-block sums of f and of the per-cube variance terms
+  const McState* state;
 };
+
+// Dynamic shared memory of mcubes_kernel: the grid, the block's histogram,
+// and one round's f^2 and bins.
+inline size_t mcubes_smem_bytes(int d, int nbins) {
+  const size_t nb1 = (size_t)nbins + 1;
+  return 2 * (size_t)d * nb1 * 8 + (size_t)kMcThreads * 8 + (size_t)d * kMcThreads * 2;
+}
 
 template <int MAXD, class Fn>
 __global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A, Fn fn) {
+  if (A.state->stop) return;  // the run has converged
   extern __shared__ __align__(16) double mc_smem[];
   const int nb1 = A.nbins + 1;
-  double* sxi = mc_smem;                 // d * nb1
-  double* hist = mc_smem + A.d * nb1;    // d * nb1 (adapt)
+  double* sxi = mc_smem;                   // d * nb1
+  double* hist = sxi + A.d * nb1;          // d * nb1 (adapt)
+  double* rf2 = hist + A.d * nb1;          // kMcThreads: this round's f^2
+  uint16_t* rbin = reinterpret_cast<uint16_t*>(rf2 + kMcThreads);  // [d][kMcThreads]: bins (0: no sample)
   for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) {
     sxi[i] = A.xi[i];
-    if (A.adapt) hist[i] = 0.0;
+    hist[i] = 0.0;
   }
   __syncthreads();
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t nthreads = (uint64_t)kMcBlocks * kMcThreads;
   const uint64_t per = (A.ncubes + nthreads - 1) / nthreads;
   const uint64_t c0 = tid * per, c1 = min(A.ncubes, c0 + per);
-  double fbg = 0.0, f2bg = 0.0;
-  for (uint64_t cube = c0; cube < c1; ++cube) {
-    // kg: 1-based interval index per axis, axis 0 most significant (get_indx, vegasT.cuh:136-154)
-    int kg[MAXD];
-    uint64_t q = cube;
+  const uint64_t mine = (c1 > c0 ? c1 - c0 : 0) * (uint64_t)A.npg;
+  const uint64_t rounds = per * (uint64_t)A.npg;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double fbg = 0.0, f2bg = 0.0, fb = 0.0, f2b = 0.0;
+  int kg[MAXD];
+  for (uint64_t round = 0; round < rounds; ++round) {
+    double f2 = 0.0;
+    int ia[MAXD];
 #pragma unroll
-    for (int j = MAXD - 1; j >= 0; --j) {
-      if (j < A.d) {
-        kg[j] = 1 + (int)(q % (uint64_t)A.ng);
-        q /= (uint64_t)A.ng;
+    for (int j = 0; j < MAXD; ++j) ia[j] = 0;
+    if (round < mine) {
+      const uint64_t cube = c0 + round / (uint64_t)A.npg;
+      const int k = 1 + (int)(round % (uint64_t)A.npg);
+      if (k == 1) {
+        // kg: 1-based interval index per axis, axis 0 most significant (get_indx, vegasT.cuh:136-154)
+        uint64_t q = cube;
+#pragma unroll
+        for (int j = MAXD - 1; j >= 0; --j) {
+          if (j < A.d) {
+            kg[j] = 1 + (int)(q % (uint64_t)A.ng);
+            q /= (uint64_t)A.ng;
+          }
+        }
       }
-    }
-    double fb = 0.0, f2b = 0.0;
-    for (int k = 1; k <= A.npg; ++k) {
       double wgt = A.xjac;
       double x[MAXD];
-      int ia[MAXD];
       uint32_t rnd[4] = {0, 0, 0, 0};
 #pragma unroll
       for (int j = 0; j < MAXD; ++j) {
@@ -122,21 +159,40 @@ __global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A, Fn fn) {
         }
       }
       const double f = __dmul_rn(wgt, fn.template eval<MAXD>(A.desc, x));
-      const double f2 = __dmul_rn(f, f);
+      f2 = __dmul_rn(f, f);
       fb = __dadd_rn(fb, f);
       f2b = __dadd_rn(f2b, f2);
-      if (A.adapt) {
-#pragma unroll
-        for (int j = 0; j < MAXD; ++j)
-          if (j < A.d) atomicAdd(&hist[j * nb1 + ia[j]], f2);
+      if (k == A.npg) {
+        // per-cube variance term (vegasT.cuh:336-343)
+        double v = sqrt(__dmul_rn(f2b, (double)A.npg));
+        v = __dmul_rn(__dsub_rn(v, fb), __dadd_rn(v, fb));
+        if (v <= 0.0) v = kTiny;
+        fbg = __dadd_rn(fbg, fb);
+        f2bg = __dadd_rn(f2bg, v);
+        fb = f2b = 0.0;
       }
     }
-    // per-cube variance term (vegasT.cuh:336-343)
-    f2b = sqrt(__dmul_rn(f2b, (double)A.npg));
-    f2b = __dmul_rn(__dsub_rn(f2b, fb), __dadd_rn(f2b, fb));
-    if (f2b <= 0.0) f2b = kTiny;
-    fbg = __dadd_rn(fbg, fb);
-    f2bg = __dadd_rn(f2bg, f2b);
+    if (A.adapt) {
+      rf2[threadIdx.x] = f2;
+#pragma unroll
+      for (int j = 0; j < MAXD; ++j)
+        if (j < A.d) rbin[j * kMcThreads + threadIdx.x] = (uint16_t)ia[j];
+      __syncthreads();
+      for (int j = warp; j < A.d; j += kMcThreads / 32) {
+        for (int i = 0; i < kMcThreads / 32; ++i) {
+          const int t = i * 32 + lane;
+          const int b = rbin[j * kMcThreads + t];
+          const unsigned peers = __match_any_sync(0xffffffffu, b);
+          if (b != 0 && lane == __ffs(peers) - 1) {
+            double s = 0.0;
+            for (unsigned m = peers; m; m &= m - 1) s = __dadd_rn(s, rf2[i * 32 + __ffs(m) - 1]);
+            hist[j * nb1 + b] = __dadd_rn(hist[j * nb1 + b], s);
+          }
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+    }
   }
   // Block sums: shuffle-down trees, then the 8 warp results in order.
   __shared__ double red[2][8];
@@ -145,7 +201,6 @@ __global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A, Fn fn) {
     fbg = __dadd_rn(fbg, __shfl_down_sync(0xffffffffu, fbg, off));
     f2bg = __dadd_rn(f2bg, __shfl_down_sync(0xffffffffu, f2bg, off));
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
     red[0][warp] = fbg;
     red[1][warp] = f2bg;
@@ -161,14 +216,12 @@ __global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A, Fn fn) {
     A.partial[2 * blockIdx.x + 1] = s1;
   }
   if (A.adapt) {
-    for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) {
-      const double v = hist[i];
-      if (v != 0.0) atomicAdd(&A.bins[i], v);
-    }
+    double* out = A.part_hist + (size_t)blockIdx.x * (size_t)(A.d * nb1);
+    for (int i = threadIdx.x; i < A.d * nb1; i += blockDim.x) out[i] = hist[i];
   }
 }
 
-// Shared memory the kernel may use: the grid and the bin histogram.
+// Shared memory the kernel may use.
 constexpr size_t kMcMaxSmem = 200 * 1024;
 
 // Host launch of one m-Cubes iteration for an integrand functor type Fn.

@@ -1173,10 +1173,11 @@ int orc_integrate(const orc::Integrand* f, double epsrel, double epsabs, const d
 // ===========================================================================
 // m-Cubes oracle.  Restates cuda_mcubes::vegas (cuda/mcubes/vegasT.cuh:643-997)
 // and its sampling kernel (vegasT.cuh:136-485) with the library's random
-// stream (Philox4x32-10, counter = cube, sample, axis pair, iteration) and
-// its work split (1024 x 256 threads, contiguous cube runs, per-thread sums,
-// 32-lane shuffle-down trees then 8 warp sums in order), so the estimate and
-// its variance match the GPU's up to the order of the f^2 bin sums.
+// stream (Philox4x32-10, counter = cube, sample, axis pair, iteration), its
+// work split (1024 x 256 threads, contiguous cube runs, per-thread sums,
+// 32-lane shuffle-down trees then 8 warp sums in order) and its order of the
+// f^2 bin sums, so the GPU's results differ from the oracle's only by the
+// last bits of exp/pow/log (CUDA's against glibc's).
 // ===========================================================================
 namespace orc {
 
@@ -1263,77 +1264,107 @@ int orc_mcubes_integrate(const orc::Integrand* f, double epsrel, double epsabs, 
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   std::vector<double> part(2 * NB);
   const int nworkers = std::max(1u, std::thread::hardware_concurrency());
+  // Per-block histograms, each formed in the library's order: rounds of one
+  // sample per thread; per round, axis by axis, batches of 32 threads in which
+  // the samples of one bin are summed in thread order before joining the bin.
+  std::vector<double> part_hist((size_t)NB * d * nb1);
   auto iteration = [&](int it, bool adapt) {
     std::fill(dbin.begin(), dbin.end(), 0.0);
-    std::vector<std::vector<double>> wbins(nworkers, std::vector<double>(adapt ? dbin.size() : 0, 0.0));
     std::vector<std::thread> th;
     for (int w = 0; w < nworkers; ++w) {
       th.emplace_back([&, w] {
-        std::vector<double>& hb = wbins[w];
+        std::vector<double> hist((size_t)d * nb1);
+        std::vector<double> rf2(NT);
+        std::vector<int> rbin((size_t)d * NT);
+        struct Lane {
+          uint64_t c0, mine;
+          double fb, f2b, fbg, f2bg;
+          int kg[kMaxDim];
+        };
+        std::vector<Lane> L(NT);
         for (int b = w; b < NB; b += nworkers) {
-          double lane_fb[NT], lane_f2b[NT];
+          std::fill(hist.begin(), hist.end(), 0.0);
           for (int t = 0; t < NT; ++t) {
             const uint64_t tid = (uint64_t)b * NT + t;
             const uint64_t c0 = tid * per, c1 = std::min(ncubes, c0 + per);
-            double fbg = 0.0, f2bg = 0.0;
-            for (uint64_t cube = c0; cube < c1; ++cube) {
-              int kg[kMaxDim];
-              uint64_t q = cube;
-              for (int j = d - 1; j >= 0; --j) {
-                kg[j] = 1 + (int)(q % ng);
-                q /= ng;
-              }
-              double fb = 0.0, f2b = 0.0;
-              for (int s = 1; s <= npg; ++s) {
-                double wgt = xjac, x[kMaxDim];
-                int ia[kMaxDim];
-                uint32_t rnd[4] = {0, 0, 0, 0};
-                for (int j = 0; j < d; ++j) {
-                  if ((j & 1) == 0) {
-                    rnd[0] = (uint32_t)cube;
-                    rnd[1] = (uint32_t)s | ((uint32_t)(cube >> 32) << 16);
-                    rnd[2] = (uint32_t)(j >> 1);
-                    rnd[3] = (uint32_t)it;
-                    philox(rnd, k0, k1);
-                  }
-                  const double ran = (j & 1) ? unit53(rnd[2], rnd[3]) : unit53(rnd[0], rnd[1]);
-                  const double xn = std::fma((double)kg[j] - ran, dxg, 1.0);
-                  const int bb = std::max(std::min((int)xn, nd), 1);
-                  const double* xij = &xi[(size_t)j * nb1];
-                  double xo, rc;
-                  if (bb > 1) {
-                    xo = xij[bb] - xij[bb - 1];
-                    rc = std::fma(xn - (double)bb, xo, xij[bb - 1]);
-                  } else {
-                    xo = xij[bb];
-                    rc = (xn - (double)bb) * xo;
-                  }
-                  x[j] = std::fma(rc, dx[j], regn[j]);
-                  wgt = wgt * (xo * xnd);
-                  ia[j] = bb;
+            L[t] = Lane{c0, (c1 > c0 ? c1 - c0 : 0) * (uint64_t)npg, 0.0, 0.0, 0.0, 0.0, {}};
+          }
+          const uint64_t rounds = per * (uint64_t)npg;
+          for (uint64_t round = 0; round < rounds; ++round) {
+            for (int t = 0; t < NT; ++t) {
+              Lane& S = L[t];
+              rf2[t] = 0.0;
+              for (int j = 0; j < d; ++j) rbin[(size_t)j * NT + t] = 0;
+              if (round >= S.mine) continue;
+              const uint64_t cube = S.c0 + round / (uint64_t)npg;
+              const int s = 1 + (int)(round % (uint64_t)npg);
+              if (s == 1) {
+                uint64_t q = cube;
+                for (int j = d - 1; j >= 0; --j) {
+                  S.kg[j] = 1 + (int)(q % ng);
+                  q /= ng;
                 }
-                const double fv = wgt * eval(P, x);
-                const double f2 = fv * fv;
-                fb = fb + fv;
-                f2b = f2b + f2;
-                if (adapt)
-                  for (int j = 0; j < d; ++j) hb[(size_t)j * nb1 + ia[j]] += f2;
               }
-              f2b = std::sqrt(f2b * (double)npg);
-              f2b = (f2b - fb) * (f2b + fb);
-              if (f2b <= 0.0) f2b = 1.0e-30;
-              fbg = fbg + fb;
-              f2bg = f2bg + f2b;
+              double wgt = xjac, x[kMaxDim];
+              uint32_t rnd[4] = {0, 0, 0, 0};
+              for (int j = 0; j < d; ++j) {
+                if ((j & 1) == 0) {
+                  rnd[0] = (uint32_t)cube;
+                  rnd[1] = (uint32_t)s | ((uint32_t)(cube >> 32) << 16);
+                  rnd[2] = (uint32_t)(j >> 1);
+                  rnd[3] = (uint32_t)it;
+                  philox(rnd, k0, k1);
+                }
+                const double ran = (j & 1) ? unit53(rnd[2], rnd[3]) : unit53(rnd[0], rnd[1]);
+                const double xn = std::fma((double)S.kg[j] - ran, dxg, 1.0);
+                const int bb = std::max(std::min((int)xn, nd), 1);
+                const double* xij = &xi[(size_t)j * nb1];
+                double xo, rc;
+                if (bb > 1) {
+                  xo = xij[bb] - xij[bb - 1];
+                  rc = std::fma(xn - (double)bb, xo, xij[bb - 1]);
+                } else {
+                  xo = xij[bb];
+                  rc = (xn - (double)bb) * xo;
+                }
+                x[j] = std::fma(rc, dx[j], regn[j]);
+                wgt = wgt * (xo * xnd);
+                rbin[(size_t)j * NT + t] = bb;
+              }
+              const double fv = wgt * eval(P, x);
+              const double f2 = fv * fv;
+              rf2[t] = f2;
+              S.fb = S.fb + fv;
+              S.f2b = S.f2b + f2;
+              if (s == npg) {
+                double v = std::sqrt(S.f2b * (double)npg);
+                v = (v - S.fb) * (v + S.fb);
+                if (v <= 0.0) v = 1.0e-30;
+                S.fbg = S.fbg + S.fb;
+                S.f2bg = S.f2bg + v;
+                S.fb = S.f2b = 0.0;
+              }
             }
-            lane_fb[t] = fbg;
-            lane_f2b[t] = f2bg;
+            if (!adapt) continue;
+            for (int j = 0; j < d; ++j)
+              for (int i = 0; i < NT / 32; ++i)
+                for (int l = 0; l < 32; ++l) {
+                  const int bb = rbin[(size_t)j * NT + i * 32 + l];
+                  bool lead = bb != 0;
+                  for (int l2 = 0; l2 < l && lead; ++l2) lead = rbin[(size_t)j * NT + i * 32 + l2] != bb;
+                  if (!lead) continue;
+                  double sum = 0.0;
+                  for (int l2 = l; l2 < 32; ++l2)
+                    if (rbin[(size_t)j * NT + i * 32 + l2] == bb) sum = sum + rf2[i * 32 + l2];
+                  hist[(size_t)j * nb1 + bb] = hist[(size_t)j * nb1 + bb] + sum;
+                }
           }
           double w0[8], w1[8];
           for (int w8 = 0; w8 < 8; ++w8) {
             double a[32], c[32];
             for (int l = 0; l < 32; ++l) {
-              a[l] = lane_fb[w8 * 32 + l];
-              c[l] = lane_f2b[w8 * 32 + l];
+              a[l] = L[w8 * 32 + l].fbg;
+              c[l] = L[w8 * 32 + l].f2bg;
             }
             for (int off = 16; off >= 1; off >>= 1)
               for (int l = 0; l < off; ++l) {
@@ -1350,13 +1381,17 @@ int orc_mcubes_integrate(const orc::Integrand* f, double epsrel, double epsabs, 
           }
           part[2 * b] = s0;
           part[2 * b + 1] = s1;
+          if (adapt) std::copy(hist.begin(), hist.end(), part_hist.begin() + (size_t)b * d * nb1);
         }
       });
     }
     for (auto& t : th) t.join();
     if (adapt)
-      for (int w = 0; w < nworkers; ++w)
-        for (size_t i = 0; i < dbin.size(); ++i) dbin[i] += wbins[w][i];
+      for (size_t i = 0; i < dbin.size(); ++i) {
+        double sum = 0.0;
+        for (int b = 0; b < NB; ++b) sum = sum + part_hist[(size_t)b * dbin.size() + i];
+        dbin[i] = sum;
+      }
     double ti = 0, tsi = 0;
     for (int b = 0; b < NB; ++b) {
       ti += part[2 * b];

@@ -1,5 +1,6 @@
 """m-Cubes on the GPU: against the CPU oracle (same Philox stream, same work
-split), against cuRAND's Philox, and on the 6-D sigma=0.01 Gaussian."""
+split, same order of the bin sums), against cuRAND's Philox, bit-for-bit
+repeatability from the seed, and on the 6-D sigma=0.01 Gaussian."""
 import os
 import shutil
 import subprocess
@@ -54,3 +55,26 @@ def test_config3_gaussian_6d(ctx):
     assert r.nregions == 14 ** 6
     assert abs(r.estimate - 1.0) <= 3 * r.errorest
     assert r.status == 0 and r.errorest <= 1e-4
+
+
+@pytest.mark.parametrize("f,ncall", [
+    (W.config3_integrand(), 2.0 ** 24),
+    (pg.genz(pg.C0, [2.0, 3.0, 1.0, 2.0], [0.5, 0.2, 0.7, 0.4]), 3e5),
+])
+def test_same_seed_repeats_bit_for_bit(ctx, f, ncall):
+    """The per-bin sums that adapt the grid are formed in a fixed order, so two
+    runs from one seed agree in every bit; another seed gives another run."""
+    runs = [ctx.mcubes_integrate(f, 1e-4, 0.0, ncall, titer=20, itmax=20, skip=5, seed=s) for s in (7, 7, 8)]
+    a, b, c = [(r.estimate, r.errorest, r.chi_sq, r.iters, r.status) for r in runs]
+    assert a == b
+    assert a != c
+
+
+def test_early_stop_counts_iterations(ctx, orc):
+    """After convergence the remaining iterations are skipped on the device:
+    the iteration count and result are those of the oracle's loop, which stops."""
+    f = pg.genz(pg.PRODUCT_PEAK, [3.0, 2.0], [0.4, 0.7])
+    r = ctx.mcubes_integrate(f, 1e-2, 0.0, 1e5, titer=30, itmax=10, skip=2, seed=3)
+    o, _ = orc.mcubes_integrate(f, 1e-2, 0.0, 1e5, titer=30, itmax=10, skip=2, seed=3)
+    assert r.status == 0 and r.iters == o.iters and r.iters < 30
+    assert abs(r.estimate - o.estimate) <= 1e-9 * abs(o.estimate)
