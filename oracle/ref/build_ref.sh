@@ -26,4 +26,14 @@ if [ -f "$HERE/ref_stages.cu" ]; then
   $NVCC -std=c++17 --expt-relaxed-constexpr -w -I"$REF" -I"$REF/externals" \
     -gencode arch=compute_103a,code=sm_103a -cubin -o "$OUT/ref_stages.cubin" "$HERE/ref_stages.cu"
 fi
+# The reference's m-Cubes sampling kernels as a cubin.
+if [ -f "$HERE/ref_mcubes.cu" ]; then
+  $NVCC -std=c++17 --expt-relaxed-constexpr -w -I"$REF" -I"$REF/externals" -I"$HERE/../.." \
+    -gencode arch=compute_103a,code=sm_103a -cubin -o "$OUT/ref_mcubes.cubin" "$HERE/ref_mcubes.cu"
+fi
+# The reference's sequential CPU m-Cubes (host program of this container).
+if [ -f "$HERE/mcubes_seq_run.cu" ]; then
+  $NVCC -std=c++17 --expt-relaxed-constexpr -w -O2 -I"$REF" -I"$REF/externals" \
+    -o "$OUT/mcubes_seq_run" "$HERE/mcubes_seq_run.cu"
+fi
 echo "build_ref: done -> $OUT"

@@ -1,0 +1,95 @@
+"""m-Cubes against the reference's own m-Cubes codes.
+
+tests/golden/mcubes_ref.json holds results of
+  "gpu": the reference's GPU m-Cubes (its own vegas_kernel / vegas_kernelF,
+         cuda/mcubes/vegasT.cuh:396-614, in its iteration loop; damping 1.5),
+         three recorded seeds per integral;
+  "seq": the reference's sequential CPU m-Cubes (cuda/mcubes/mcubesSeq.hh;
+         damping 0.5, every iteration adapts and enters the weighted mean),
+         three recorded seeds for two small integrals, one for the 6-D Gaussian,
+made by tests/golden/make_mcubes_ref_golden.py.  Both codes draw different
+random numbers from the library's, so agreement is statistical, with the same
+call budget, iteration counts and damping.
+
+The reference's GPU code seeds cuRAND with curand_init(seed, blockIdx.x,
+threadIdx.x, ...) (cuda/mcubes/util/vegas_utils.cuh:62-65): the thread index
+is the offset, so the threads of a block draw from one sequence shifted by one
+number each, their samples are correlated, and its reported standard
+deviations are too small (its runs of the 3-D corner peak lie 4.5 and 4.0
+reported deviations from the exact value).  Its three runs per integral are
+therefore compared through their mean and the larger of the propagated
+deviation and the runs' own standard error; the library (independent Philox
+streams) must lie within 3 combined deviations of that mean, and within 3 of
+its own deviations of the exact value.  The sequential code's runs are
+compared run by run.  Its 6-D Gaussian run is recorded but not compared: its
+weighted mean includes the first, unadapted iterations (no skip), whose
+variance estimates are unreliable for a peak of width 0.01, and it lies 3.2
+standard deviations from the exact value 1.
+"""
+import json
+import math
+import os
+
+import pytest
+
+import gpuintegration_gb300 as pg
+from gpuintegration_gb300 import workloads as W
+
+PATH = os.path.join(os.path.dirname(__file__), "golden", "mcubes_ref.json")
+GOLD = json.load(open(PATH)) if os.path.exists(PATH) else {}
+CASES = {"gauss6_sigma0.01": W.config3_integrand(),
+         "corner3": pg.genz(pg.CORNER_PEAK, [3.0, 2.0, 1.0], [0.0, 0.0, 0.0]),
+         "c0_4": pg.genz(pg.C0, [2.0, 3.0, 1.0, 2.0], [0.5, 0.2, 0.7, 0.4])}
+EXACT = {"gauss6_sigma0.01": 1.0, "corner3": W.analytic(CASES["corner3"]), "c0_4": W.analytic(CASES["c0_4"])}
+
+
+def _agree(a, sa, b, sb, k=3.0):
+    return abs(a - b) <= k * math.hypot(sa, sb)
+
+
+def _gpu_reference(case):
+    """Mean of the reference GPU runs of `case` and its standard error (the
+    larger of the propagated reported deviations and the runs' spread)."""
+    est = [r["estimate"] for r in GOLD["gpu"] if r["case"] == case]
+    err = [r["errorest"] for r in GOLD["gpu"] if r["case"] == case]
+    n = len(est)
+    mean = sum(est) / n
+    spread = math.sqrt(sum((e - mean) ** 2 for e in est) / (n - 1)) / math.sqrt(n)
+    return mean, max(math.sqrt(sum(e * e for e in err)) / n, spread)
+
+
+@pytest.mark.skipif("gpu" not in GOLD or "seq" not in GOLD, reason="reference m-Cubes results not generated")
+def test_reference_runs_meet_the_exact_values():
+    for case in CASES:
+        mean, sem = _gpu_reference(case)
+        assert _agree(mean, sem, EXACT[case], 0.0), case
+    for r in GOLD["seq"]:
+        if r["case"] != "gauss6_sigma0.01":
+            assert _agree(r["estimate"], r["errorest"], EXACT[r["case"]], 0.0), r
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif("gpu" not in GOLD, reason="reference GPU m-Cubes results not generated")
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_library_agrees_with_reference_gpu_mcubes(ctx, case):
+    r0 = [r for r in GOLD["gpu"] if r["case"] == case][0]
+    mean, sem = _gpu_reference(case)
+    for seed in (1, 2):
+        res = ctx.mcubes_integrate(CASES[case], r0["epsrel"], 0.0, r0["ncall"], titer=r0["titer"], itmax=r0["itmax"],
+                                   skip=r0["skip"], seed=seed, alpha=1.5)
+        assert _agree(res.estimate, res.errorest, mean, sem), (case, seed, res, mean, sem)
+        assert _agree(res.estimate, res.errorest, EXACT[case], 0.0), (case, seed, res)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif("seq" not in GOLD, reason="reference sequential m-Cubes results not generated")
+@pytest.mark.parametrize("case", ["corner3", "c0_4"])
+def test_library_agrees_with_reference_sequential_mcubes(ctx, case):
+    refs = [r for r in GOLD["seq"] if r["case"] == case]
+    r0 = refs[0]
+    # every iteration adapts and enters the mean, damping 0.5, no early stop: the sequential code's loop
+    res = ctx.mcubes_integrate(CASES[case], 1e-12, 0.0, r0["ncall"], titer=r0["itmx"], itmax=r0["itmx"], skip=0,
+                               seed=5, alpha=0.5)
+    assert res.iters == r0["itmx"]
+    for r in refs:
+        assert _agree(res.estimate, res.errorest, r["estimate"], r["errorest"]), (case, res, r)
