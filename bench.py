@@ -542,7 +542,9 @@ def run_batched(args, rank, world, local, t_begin):
             "regions_per_step": st.regions_evaluated // args.steps,
             "step_breakdown_ms": {"evaluation": st.eval_ms / args.steps, "stages": st.stage_ms / args.steps,
                                   "host_decisions": st.host_ms / args.steps, "spill": st.spill_ms / args.steps,
-                                  "admission": st.admit_ms / args.steps},
+                                  "admission": st.admit_ms / args.steps,
+                                  "classifier_host": st.classify_ms / args.steps,
+                                  "classifier_passes": st.classify_passes / args.steps},
             "setsum_region_share": st.setsum_regions / max(st.regions_evaluated, 1),
             "iterations": iteration_summary(ctx.iterations(), args.steps)}
     if rank == 0:

@@ -77,7 +77,8 @@ class PgStats(ctypes.Structure):
                 ("tune_warps", ctypes.c_int32 * 2), ("tune_ctas_per_sm", ctypes.c_int32 * 2),
                 ("eval_bytes", ctypes.c_uint64), ("host_ms", ctypes.c_double), ("sync_ms", ctypes.c_double),
                 ("spill_ms", ctypes.c_double), ("admit_ms", ctypes.c_double),
-                ("setsum_regions", ctypes.c_uint64)]
+                ("setsum_regions", ctypes.c_uint64), ("classify_ms", ctypes.c_double),
+                ("classify_passes", ctypes.c_uint64)]
 
 
 class PgIterationRecord(ctypes.Structure):

@@ -149,11 +149,11 @@ Engine::~Engine() {
   DevBuf* dev_bufs[] = {&rule_trie_, &rule_leafset_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
                         &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
                         &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
-                        &thr_out_, &adm_starts_, &adm_ids_, &sp_left_, &sp_len_, &sp_par_};
+                        &thr_out_, &thr_counts_, &adm_starts_, &adm_ids_, &rst_items_};
   for (DevBuf* b : dev_bufs)
     if (b->p) cudaFree(b->p);
   DevBuf* host_bufs[] = {&h_segs_, &h_chunks_, &h_trans_, &h_trans_spill_, &h_scal_, &h_live_, &h_thr_,
-                         &h_adm_starts_, &h_adm_ids_};
+                         &h_adm_starts_, &h_adm_ids_, &h_rst_items_, &h_thr_counts_};
   for (DevBuf* b : host_bufs)
     if (b->p) cudaFreeHost(b->p);
   for (auto& e : ev_)
@@ -340,7 +340,9 @@ int Engine::init(std::string* why) {
   R.scale = (const double*)rule_scale_.p;
   R.norm = (const double*)rule_norm_.p;
   rule_ = R;
-  if ((rc = ensure(thr_out_, 64)) != PG_OK || (rc = ensure_pinned(h_thr_, 64)) != PG_OK) {
+  if ((rc = ensure(thr_out_, 64)) != PG_OK || (rc = ensure_pinned(h_thr_, 64)) != PG_OK ||
+      (rc = ensure(thr_counts_, kMaxThresholds * 8)) != PG_OK ||
+      (rc = ensure_pinned(h_thr_counts_, kMaxThresholds * 8)) != PG_OK) {
     if (why) *why = last_error;
     return rc;
   }
@@ -400,8 +402,38 @@ int Engine::threshold_pass(uint32_t jidx, double thr, int write_flags, int minma
   PG_TRY(cudaMemcpyAsync(h_thr_.p, thr_out_.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
          "threshold readback");
   PG_TRY(cudaStreamSynchronize(stream_), "threshold pass");
+  stats.classify_passes++;
   std::memcpy(out, h_thr_.p, 5 * sizeof(double));
   stats.d2h_bytes += 5 * sizeof(double);
+  return PG_OK;
+}
+
+int Engine::threshold_counts(uint32_t jidx, const double* thr, int k, uint64_t* counts) {
+  const SegDesc& S = ((const SegDesc*)h_segs_.p)[jidx];
+  ThresholdSet ts;
+  std::memset(&ts, 0, sizeof ts);
+  ts.k = k;
+  for (int q = 0; q < k; ++q) {
+    if (!(thr[q] >= 0.0)) {  // the kernel compares bit patterns of non-negative values
+      last_error = "negative threshold";
+      return PG_BAD_ARG;
+    }
+    const double t = thr[q] + 0.0;  // +0 for a -0 threshold
+    std::memcpy(&ts.bits[q], &t, 8);
+  }
+  PG_TRY(cudaMemsetAsync(thr_counts_.p, 0, kMaxThresholds * 8, stream_), "threshold counts");
+  if (S.nchunks) {
+    threshold_count_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(
+        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, S.chunk_start, (const double*)err_b_.p, ts,
+        (unsigned long long*)thr_counts_.p);
+    stats.launches++;
+  }
+  PG_TRY(cudaGetLastError(), "threshold count launch");
+  PG_TRY(cudaMemcpyAsync(h_thr_counts_.p, thr_counts_.p, k * 8, cudaMemcpyDeviceToHost, stream_), "count readback");
+  PG_TRY(cudaStreamSynchronize(stream_), "threshold counts");
+  stats.classify_passes++;
+  std::memcpy(counts, h_thr_counts_.p, k * 8);
+  stats.d2h_bytes += k * 8;
   return PG_OK;
 }
 
@@ -414,6 +446,7 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
   const uint64_t n = J.n;
   double o[5];
   int rc;
+  const auto t_cls = std::chrono::steady_clock::now();
   if ((rc = threshold_pass(jidx, INFINITY, 0, 1, 0, o)) != PG_OK) return rc;
   const double mn = o[3], mx = o[4];
   double low = mn, high = mx, thr = iter_err / (double)n, flags_thr = thr;
@@ -435,7 +468,7 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
     return PG_OK;
   };
   do {
-    if (!pass_mem && inc <= 20) {
+    if (!pass_mem && inc <= 20 && !(thr >= 0.0)) {  // (never: thresholds are error values) one pass each
       pass_mem = false;
       for (uint64_t cnt = 0; !pass_mem && cnt < 20; ++cnt) {
         if ((rc = apply(thr)) != PG_OK) return rc;
@@ -443,6 +476,33 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
           low = thr;
           thr += std::fabs(high - thr) * .5;
         }
+      }
+      inc++;
+    } else if (!pass_mem && inc <= 20) {
+      // The reference raises the threshold up to 20 times until few enough
+      // regions stay active (heuristic_classifier.cuh:380-395).  The
+      // thresholds it tries do not depend on the outcomes, and the test needs
+      // only the count above each, so all 20 counts come from one pass; the
+      // full pass then runs at the threshold where the search stops.
+      double seq[kMaxThresholds];
+      double t = thr;
+      for (int q = 0; q < kMaxThresholds; ++q) {
+        seq[q] = t;
+        t += std::fabs(high - t) * .5;
+      }
+      uint64_t cnt[kMaxThresholds];
+      if ((rc = threshold_counts(jidx, seq, kMaxThresholds, cnt)) != PG_OK) return rc;
+      int stop = -1;
+      for (int q = 0; q < kMaxThresholds && stop < 0; ++q)
+        if ((double)(int)cnt[q] / (double)(int)n <= C.max_active_regions_percentage) stop = q;
+      const int last = stop >= 0 ? stop : kMaxThresholds - 1;
+      if ((rc = apply(seq[last])) != PG_OK) return rc;
+      if (stop >= 0) {
+        if (stop > 0) low = seq[stop - 1];
+        thr = seq[stop];
+      } else {
+        low = seq[last];
+        thr = t;  // the threshold after the 20th
       }
       inc++;
     }
@@ -474,6 +534,7 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
   C.max_active_regions_percentage = .5;
   C.max_percent_error_budget = .25;
   const bool ok = pass_mem && pass_budget;
+  stats.classify_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_cls).count();
   *ok_out = ok;
   *num_active_out = num_active;
   if (ok) {
@@ -771,29 +832,52 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
           PG_TRY(cudaGetLastError(), "initial regions launch");
           stats.h2d_bytes += J.n * 16 * d;
         }
-        for (uint32_t j : restore) {
-          Job& J = jobs[j];
-          const int d = J.desc.d;
-          SpillBatch& B = spill_batches_[J.sp_batch];
-          const double* sl = B.p + J.sp_off;
-          const double* sn = B.p + (uint64_t)B.rows * B.stride + J.sp_off;
-          const double* sq = B.p + 2ull * B.rows * B.stride + J.sp_poff;
-          PG_TRY(cudaMemcpy2DAsync((double*)left_[cur].p + J.start, reg_cap_[cur] * 8, sl, B.stride * 8, J.n * 8, d,
-                                   cudaMemcpyHostToDevice, stream_), "restore");
-          PG_TRY(cudaMemcpy2DAsync((double*)len_[cur].p + J.start, reg_cap_[cur] * 8, sn, B.stride * 8, J.n * 8, d,
-                                   cudaMemcpyHostToDevice, stream_), "restore");
-          PG_TRY(cudaMemcpyAsync((double*)parent_[cur].p + J.par_start, sq, (J.n / 2) * 8, cudaMemcpyHostToDevice,
-                                 stream_), "restore");
-          fill_owner_kernel<<<(unsigned)div_up(J.n, 256), 256, 0, stream_>>>((uint32_t*)owner_[cur].p, J.start, J.n,
-                                                                            j);
+        // Restores: one kernel reads every restored integral's list straight
+        // from its pinned slice (the table's host mirror is rewritten only
+        // after the iteration's synchronisation, so its last upload is done).
+        if (!restore.empty()) {
+          if ((rc = ensure(rst_items_, restore.size() * sizeof(RestoreItem))) != PG_OK) return rc;
+          if ((rc = ensure_pinned(h_rst_items_, restore.size() * sizeof(RestoreItem))) != PG_OK) return rc;
+          RestoreItem* items = (RestoreItem*)h_rst_items_.p;
+          uint64_t blocks = 0;
+          for (size_t q = 0; q < restore.size(); ++q) {
+            Job& J = jobs[restore[q]];
+            SpillBatch& B = spill_batches_[J.sp_batch];
+            RestoreItem& I = items[q];
+            I.src_left = B.dp + J.sp_off;
+            I.src_len = B.dp + (uint64_t)B.rows * B.stride + J.sp_off;
+            I.src_par = B.dp + 2ull * B.rows * B.stride + J.sp_poff;
+            I.src_stride = B.stride;
+            I.start = J.start;
+            I.par_start = J.par_start;
+            I.n = J.n;
+            I.block0 = blocks;
+            I.owner = restore[q];
+            I.d = J.desc.d;
+            blocks += div_up(J.n, kRestoreRegions);
+            stats.h2d_bytes += J.n * 16 * (uint64_t)J.desc.d + (J.n / 2) * 8;
+          }
+          PG_TRY(cudaMemcpyAsync(rst_items_.p, items, restore.size() * sizeof(RestoreItem), cudaMemcpyHostToDevice,
+                                 stream_), "restore table");
+          if (blocks > 0x7fffffffull) {
+            last_error = "restore grid too large";
+            return PG_BAD_ARG;
+          }
+          restore_kernel<<<(unsigned)blocks, 256, 0, stream_>>>((const RestoreItem*)rst_items_.p,
+                                                                (uint32_t)restore.size(), (double*)left_[cur].p,
+                                                                (double*)len_[cur].p, reg_cap_[cur],
+                                                                (uint32_t*)owner_[cur].p, (double*)parent_[cur].p);
           stats.launches++;
           PG_TRY(cudaGetLastError(), "restore launch");
-          stats.h2d_bytes += J.n * 16 * d + J.n * 4;
-          // When the batch's last integral is back, its slice may be handed out
-          // again at once: the next writer is a copy queued behind these on the
-          // same stream.
-          if (--B.live == 0) spill_.release(B.p, B.bytes);
-          J.sp_batch = -1;
+          // When a batch's last integral is back, its slice may be handed out
+          // again at once: the next writer is a kernel queued behind this one
+          // on the same stream.
+          for (uint32_t j : restore) {
+            Job& J = jobs[j];
+            SpillBatch& B = spill_batches_[J.sp_batch];
+            if (--B.live == 0) spill_.release(B.p, B.bytes);
+            J.sp_batch = -1;
+          }
         }
         if (profiling) cudaEventRecord(ev_[9], stream_);
         T = t;
@@ -1049,7 +1133,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       // groups [gbeg[g], gbeg[g+1]) of the spill list, with their region and parent totals
       std::vector<size_t> gbeg{0};
       std::vector<uint64_t> gsst, gspt;
-      uint64_t sst = 0, spt = 0, max_sst = 0, max_spt = 0;
+      uint64_t sst = 0, spt = 0;
       std::memcpy(hsp, ht, njobs * sizeof(Transition));
       for (uint32_t j = 0; j < njobs; ++j) hsp[j].mode = 0;
       for (size_t q = 0; q < spill.size(); ++q) {
@@ -1068,16 +1152,11 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
         jobs[j].sp_poff = spt;
         sst += n2;
         spt += keepA[j];
-        max_sst = std::max(max_sst, sst);
-        max_spt = std::max(max_spt, spt);
         ht[j].mode = 0;
       }
       gsst.push_back(sst);
       gspt.push_back(spt);
       gbeg.push_back(spill.size());
-      if ((rc = ensure(sp_left_, max_sst * maxd * 8)) != PG_OK) return rc;
-      if ((rc = ensure(sp_len_, max_sst * maxd * 8)) != PG_OK) return rc;
-      if ((rc = ensure(sp_par_, max_spt * 8)) != PG_OK) return rc;
       PG_TRY(cudaMemcpyAsync(trans_.p, hsp, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
              "transition upload");
       stats.h2d_bytes += njobs * sizeof(Transition);
@@ -1085,9 +1164,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
         const uint32_t jf = spill[gbeg[g]], jl = spill[gbeg[g + 1] - 1];
         const uint32_t c0 = hs[jf].chunk_start, c1 = hs[jl].chunk_start + hs[jl].nchunks;
         const uint64_t st = gsst[g], pt = gspt[g];
-        if ((rc = compact(cur, cur ^ 1, c0, c1 - c0, maxd, (double*)sp_left_.p, (double*)sp_len_.p, st, nullptr,
-                          (double*)sp_par_.p)) != PG_OK)
-          return rc;
+        // The group's children and parents go straight into a pinned slice:
+        // the compaction writes host memory over NVLink-C2C.
         SpillBatch B;
         B.bytes = (2 * st * (uint64_t)maxd + pt) * 8;
         B.p = (double*)spill_.alloc(B.bytes);
@@ -1098,9 +1176,12 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
           last_error = "pinned host memory for spilled region lists";
           return PG_OOM;
         }
-        PG_TRY(cudaMemcpyAsync(B.p, sp_left_.p, st * maxd * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-        PG_TRY(cudaMemcpyAsync(B.p + st * maxd, sp_len_.p, st * maxd * 8, cudaMemcpyDeviceToHost, stream_), "spill");
-        PG_TRY(cudaMemcpyAsync(B.p + 2 * st * maxd, sp_par_.p, pt * 8, cudaMemcpyDeviceToHost, stream_), "spill");
+        void* dp = nullptr;
+        PG_TRY(cudaHostGetDevicePointer(&dp, B.p, 0), "device address of a pinned slice");
+        B.dp = (double*)dp;
+        if ((rc = compact(cur, cur ^ 1, c0, c1 - c0, maxd, B.dp, B.dp + st * maxd, st, nullptr,
+                          B.dp + 2 * st * maxd)) != PG_OK)
+          return rc;
         stats.d2h_bytes += st * maxd * 16 + pt * 8;
         const int bidx = (int)spill_batches_.size();
         spill_batches_.push_back(B);

@@ -232,6 +232,8 @@ class Engine {
   int classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err, bool* ok, double* fin_est_out,
                    double* fin_err_out, uint64_t* num_active, double iter_est);
   int threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5]);
+  // Counts of integral jidx's errors above each of the k thresholds (one pass).
+  int threshold_counts(uint32_t jidx, const double* thr, int k, uint64_t* counts);
   int grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_t live_par);
   int compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
               uint64_t out_stride, uint32_t* out_owner, double* parent_out);
@@ -253,14 +255,15 @@ class Engine {
   // per-chunk
   DevBuf partials_, chunk_off_, chunks_;
   // per-integral
-  DevBuf segs_, trans_, descs_, scal_, live_, thr_out_, adm_starts_, adm_ids_;
-  // transient device copy of one job's next list on its way to host memory
-  DevBuf sp_left_, sp_len_, sp_par_;
+  DevBuf segs_, trans_, descs_, scal_, live_, thr_out_, thr_counts_, adm_starts_, adm_ids_;
+  // restore table of one admission (device, and its pinned host mirror)
+  DevBuf rst_items_, h_rst_items_;
   SpillArena spill_;
   // Spill batches of the current run: slice, its size, rows and row stride
   // (regions) of its region block, and the number of integrals still in it.
   struct SpillBatch {
     double* p;
+    double* dp;  // the same slice as the device addresses it
     size_t bytes;
     int rows;
     uint64_t stride;
@@ -269,7 +272,8 @@ class Engine {
   std::vector<SpillBatch> spill_batches_;
   bool compact_timing_pending_ = false;
   // pinned host mirrors
-  DevBuf h_segs_, h_chunks_, h_trans_, h_trans_spill_, h_scal_, h_live_, h_thr_, h_adm_starts_, h_adm_ids_;
+  DevBuf h_segs_, h_chunks_, h_trans_, h_trans_spill_, h_scal_, h_live_, h_thr_, h_thr_counts_, h_adm_starts_,
+      h_adm_ids_;
   // 0-1 evaluation, 1-2 stages, 4-5 compaction, 6-7 spills, 8-9 admission and restores
   cudaEvent_t ev_[10] = {};
   bool spill_timing_pending_ = false, admit_timing_pending_ = false;

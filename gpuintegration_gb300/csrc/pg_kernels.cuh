@@ -211,9 +211,14 @@ static __global__ void __launch_bounds__(kRedThreads)
 // bisection (Sub_region_splitter.cuh:8-46).  Kept region k of integral j gives
 // child 0 at out_start + k and child 1 at out_start + A + k; the parent
 // estimate goes to par_out + k for the next two-level step.
+//
+// A chunk of 2048 regions is taken as 8 slices of 256, one region per thread
+// and slice, so a warp's loads of the SoA rows and its stores of the children
+// are consecutive addresses.  The kept regions' order is the list order:
+// slice by slice, and inside a slice by a warp ballot and the 8 warps' counts.
 // ---------------------------------------------------------------------------
 template <int MAXD>
-static __global__ void __launch_bounds__(kRedThreads)
+static __global__ void __launch_bounds__(kRedThreads, 3)
     compact_split_kernel(const ChunkRef* __restrict__ chunks, const SegDesc* __restrict__ segs,
                          const Transition* __restrict__ trans, const uint64_t* __restrict__ chunk_off,
                          const IntegralDesc* __restrict__ descs, const uint8_t* __restrict__ active,
@@ -221,56 +226,71 @@ static __global__ void __launch_bounds__(kRedThreads)
                          const int32_t* __restrict__ bisect, const double* __restrict__ est,
                          double* __restrict__ out_left, double* __restrict__ out_length, uint64_t out_stride,
                          uint32_t* __restrict__ out_owner, double* __restrict__ parent_out, uint32_t chunk0) {
-  __shared__ uint64_t sc[33];
+  __shared__ uint32_t wcount[kRedThreads / 32];
   const uint32_t cidx = chunk0 + blockIdx.x;
   const ChunkRef cr = chunks[cidx];
   const Transition T = trans[cr.integral];
   if (T.mode == 0) return;
   const SegDesc S = segs[cr.integral];
   const int d = descs[cr.integral].d;
-  const uint64_t first = (uint64_t)cr.local * kChunk + (uint64_t)threadIdx.x * kRedItems;
-  uint8_t keep[kRedItems];
-  uint64_t cnt = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t chunk_first = (uint64_t)cr.local * kChunk;
+  // kept regions of this integral before the chunk
+  uint64_t run = (T.mode == 2) ? chunk_first : chunk_off[cidx];
+#pragma unroll 1
+  for (int k = 0; k < kRedItems; ++k) {
+    const uint64_t li = chunk_first + (uint64_t)k * kRedThreads + threadIdx.x;
+    const bool keep = li < S.n && (T.mode == 2 || active[S.start + li]);
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wcount[warp] = __popc(mask);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
 #pragma unroll
-  for (int q = 0; q < kRedItems; ++q) {
-    const uint64_t li = first + q;
-    keep[q] = (li < S.n) ? ((T.mode == 2) ? 1 : active[S.start + li]) : 0;
-    cnt += keep[q];
-  }
-  uint64_t total;
-  uint64_t pos = block_exclusive_scan(cnt, sc, &total);
-  pos += (T.mode == 2) ? (uint64_t)cr.local * kChunk : chunk_off[cidx];
+    for (int w = 0; w < kRedThreads / 32; ++w) {
+      const uint32_t c = wcount[w];
+      before += (w < warp) ? c : 0u;
+      total += c;
+    }
+    if (keep) {
+      const uint64_t pos = run + before + __popc(mask & ((1u << lane) - 1u));
+      const uint64_t i = S.start + li;
+      const uint64_t c0 = T.out_start + pos, c1 = T.out_start + T.A + pos;
+      const int bd = bisect[i];
+      // every load of the region before any store: 2d loads in flight per thread
+      double l[MAXD], h[MAXD];
 #pragma unroll
-  for (int q = 0; q < kRedItems; ++q) {
-    if (!keep[q]) continue;
-    const uint64_t i = S.start + first + q;
-    const uint64_t k = pos++;
-    const uint64_t c0 = T.out_start + k, c1 = T.out_start + T.A + k;
-    const int bd = bisect[i];
-#pragma unroll
-    for (int dim = 0; dim < MAXD; ++dim) {
-      if (dim < d) {
-        const double l = left[(uint64_t)dim * stride + i];
-        const double h = length[(uint64_t)dim * stride + i];
-        if (dim == bd) {
-          const double hh = __ddiv_rn(h, 2.0);
-          out_left[(uint64_t)dim * out_stride + c0] = __dadd_rn(l, __dmul_rn(0.0, hh));
-          out_left[(uint64_t)dim * out_stride + c1] = __dadd_rn(l, __dmul_rn(1.0, hh));
-          out_length[(uint64_t)dim * out_stride + c0] = hh;
-          out_length[(uint64_t)dim * out_stride + c1] = hh;
-        } else {
-          out_left[(uint64_t)dim * out_stride + c0] = l;
-          out_left[(uint64_t)dim * out_stride + c1] = l;
-          out_length[(uint64_t)dim * out_stride + c0] = h;
-          out_length[(uint64_t)dim * out_stride + c1] = h;
+      for (int dim = 0; dim < MAXD; ++dim) {
+        if (dim < d) {
+          l[dim] = left[(uint64_t)dim * stride + i];
+          h[dim] = length[(uint64_t)dim * stride + i];
         }
       }
+      const double e = est[i];
+#pragma unroll
+      for (int dim = 0; dim < MAXD; ++dim) {
+        if (dim < d) {
+          if (dim == bd) {
+            const double hh = __ddiv_rn(h[dim], 2.0);
+            out_left[(uint64_t)dim * out_stride + c0] = __dadd_rn(l[dim], __dmul_rn(0.0, hh));
+            out_left[(uint64_t)dim * out_stride + c1] = __dadd_rn(l[dim], __dmul_rn(1.0, hh));
+            out_length[(uint64_t)dim * out_stride + c0] = hh;
+            out_length[(uint64_t)dim * out_stride + c1] = hh;
+          } else {
+            out_left[(uint64_t)dim * out_stride + c0] = l[dim];
+            out_left[(uint64_t)dim * out_stride + c1] = l[dim];
+            out_length[(uint64_t)dim * out_stride + c0] = h[dim];
+            out_length[(uint64_t)dim * out_stride + c1] = h[dim];
+          }
+        }
+      }
+      if (out_owner) {
+        out_owner[c0] = cr.integral;
+        out_owner[c1] = cr.integral;
+      }
+      parent_out[T.par_out + pos] = e;
     }
-    if (out_owner) {
-      out_owner[c0] = cr.integral;
-      out_owner[c1] = cr.integral;
-    }
-    parent_out[T.par_out + k] = est[i];
+    run += total;
+    __syncthreads();  // wcount is rewritten by the next slice
   }
 }
 
@@ -337,6 +357,49 @@ static __global__ void __launch_bounds__(kRedThreads)
     P.q[3] = ns_zero();
     P.count = cnt_s;
   }
+}
+
+// Counts of one integral's errors above each of up to kMaxThresholds
+// thresholds (the memory-pressure classifier's stopping test needs only the
+// count): integer totals, added with atomics, so the order does not matter.
+// The thresholds are non-negative, so for a non-negative error the comparison
+// is one on bit patterns; a NaN or negative-signed error exceeds none of them,
+// as in threshold_kernel.
+constexpr int kMaxThresholds = 20;
+struct ThresholdSet {
+  unsigned long long bits[kMaxThresholds];
+  int k;
+};
+
+static __global__ void __launch_bounds__(kRedThreads)
+    threshold_count_kernel(const ChunkRef* __restrict__ chunks, const SegDesc* __restrict__ segs, uint32_t chunk0,
+                           const double* __restrict__ err, ThresholdSet ts, unsigned long long* __restrict__ counts) {
+  __shared__ unsigned long long sc[kMaxThresholds];
+  if (threadIdx.x < kMaxThresholds) sc[threadIdx.x] = 0ull;
+  __syncthreads();
+  const ChunkRef cr = chunks[chunk0 + blockIdx.x];
+  const SegDesc S = segs[cr.integral];
+  uint32_t c[kMaxThresholds];
+#pragma unroll
+  for (int q = 0; q < kMaxThresholds; ++q) c[q] = 0;
+#pragma unroll
+  for (int k = 0; k < kRedItems; ++k) {
+    const uint64_t li = (uint64_t)cr.local * kChunk + (uint64_t)k * kRedThreads + threadIdx.x;
+    if (li < S.n) {
+      const unsigned long long e = (unsigned long long)__double_as_longlong(err[S.start + li]);
+      if (e <= 0x7ff0000000000000ull) {  // not NaN, sign bit clear
+#pragma unroll
+        for (int q = 0; q < kMaxThresholds; ++q) c[q] += (q < ts.k && e > ts.bits[q]) ? 1u : 0u;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kMaxThresholds; ++q) {
+    const unsigned v = __reduce_add_sync(0xffffffffu, c[q]);
+    if ((threadIdx.x & 31) == 0 && q < ts.k && v) atomicAdd(&sc[q], (unsigned long long)v);
+  }
+  __syncthreads();
+  if (threadIdx.x < ts.k && sc[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
 }
 
 // Merge of threshold partials of one integral (same order as finalize_kernel)
@@ -457,6 +520,47 @@ static __global__ void uniform_split_batch_kernel(double* __restrict__ left, dou
     length[(uint64_t)k * stride + r] = len;
   }
   owner[r] = j;
+}
+
+// One spilled integral's way back into the list: its rows (left, length),
+// parent estimates and owner.  src_* point at a pinned host slice the device
+// reads directly (NVLink-C2C on Grace); block0 is its first block.
+struct RestoreItem {
+  const double* src_left;
+  const double* src_len;
+  const double* src_par;
+  uint64_t src_stride;
+  uint64_t start, par_start, n;
+  uint64_t block0;
+  uint32_t owner;
+  int32_t d;
+};
+
+constexpr int kRestoreRegions = 1024;  // regions per block of restore_kernel
+
+// Every integral restored in one admission, one kernel: block b serves the
+// item with the largest block0 <= b, regions [1024 (b - block0), +1024).
+static __global__ void __launch_bounds__(256)
+    restore_kernel(const RestoreItem* __restrict__ items, uint32_t nitems, double* __restrict__ left,
+                   double* __restrict__ length, uint64_t stride, uint32_t* __restrict__ owner,
+                   double* __restrict__ parent) {
+  uint32_t lo = 0, hi = nitems;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (items[mid].block0 <= blockIdx.x) lo = mid; else hi = mid;
+  }
+  const RestoreItem I = items[lo];
+  const uint64_t base = (uint64_t)(blockIdx.x - I.block0) * kRestoreRegions;
+  for (int q = 0; q < kRestoreRegions / 256; ++q) {
+    const uint64_t k = base + (uint64_t)q * 256 + threadIdx.x;
+    if (k >= I.n) break;
+    for (int dim = 0; dim < I.d; ++dim) {
+      left[(uint64_t)dim * stride + I.start + k] = I.src_left[(uint64_t)dim * I.src_stride + k];
+      length[(uint64_t)dim * stride + I.start + k] = I.src_len[(uint64_t)dim * I.src_stride + k];
+    }
+    owner[I.start + k] = I.owner;
+    if (k < I.n / 2) parent[I.par_start + k] = I.src_par[k];
+  }
 }
 
 static __global__ void fill_owner_kernel(uint32_t* __restrict__ owner, uint64_t start, uint64_t n, uint32_t j) {

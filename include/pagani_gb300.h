@@ -149,6 +149,8 @@ typedef struct pg_stats {
   double spill_ms;              /* device time of moving region lists out of the pool (compaction + copies) */
   double admit_ms;              /* device time of admissions: first splits and region lists moved back in */
   uint64_t setsum_regions;      /* regions evaluated by generator-set sums (PG_EVAL_SET_SUMS) */
+  double classify_ms;           /* host time in the memory-pressure classifier (its passes included) */
+  uint64_t classify_passes;     /* threshold passes of the classifier (each a launch and a readback) */
 } pg_stats;
 
 /* One iteration of a run (recorded while profiling is on): regions in the
