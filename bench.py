@@ -92,6 +92,11 @@ def _feval(d):
     return 1 + 8 * d + 2 * d * (d - 1) + 4 * d * (d - 1) + 4 * d * (d - 1) * (d - 2) // 3 + (1 << d)
 
 
+def _first_split(d):
+    """Regions of an integral's first list (the uniform split)."""
+    return (4 if d < 5 else (2 if d <= 10 else 1)) ** d
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -155,8 +160,10 @@ def load_screen():
 # The driver's peak file holds HBM and bf16 figures only.  A libm call or a
 # division counts the FP64 instructions it executes on this GPU, measured by
 # ncu (smsp__sass_thread_inst_executed_op_fp64_pred_on per region, less the
-# counted arithmetic: profiles/setsum_kernel_fp64_mix.md).  Multiplies the
-# kernels run on the integer pipe (pg::mul_rn_int) are not FP64 operations.
+# counted arithmetic: profiles/setsum_kernel_fp64_mix.md).  The set-sum
+# kernel's multiplies run on the FP64 pipe and are counted; the point-by-point
+# kernel's products of the point values run on the integer pipe
+# (pg::mul_rn_int) and are not.
 LIBM_OPS = {"exp": 17.2, "div": 6.2, "cos": 22.0}
 
 
@@ -169,12 +176,35 @@ def _factor_ops(family):
             pg.PRODUCT: 0}.get(family, 0)
 
 
-def setsum_ops(family, d, unit=True):
-    """FP64 operations of one region of setsum_kernel (PG_EVAL_SET_SUMS): per axis 11
-    coordinates (1 FMA, 2 off the unit cube), 11 factors, 5 pair sums, 8 recurrence FMAs;
-    per region 40 rule-sum FMAs, the fourth differences (5 d + 1) and 27 null-rule FMAs plus 6."""
-    axis = 11 * (1 if unit else 2) + 11 * _factor_ops(family) + 5 + 8
-    return d * axis + 40 + (5 * d + 1) + 27 + 6
+def _fd_products(d):
+    """Multiplies of the fourth differences' point values (two half products per point)."""
+    m = d // 2
+    n = (m - 1) + (d - m - 1) + 1            # the centre's half products and L * R
+    for k in range(d):
+        hbeg, hend = (0, m) if k < m else (m, d)
+        n += 4 * (k != hbeg) + 4 * (hend - k - 1) + 4 + (k != hbeg)
+    return n
+
+
+def setsum_ops(family, d, unit=True, paired=0.0, cached=0.0):
+    """FP64 operations per region of setsum_kernel (PG_EVAL_SET_SUMS).  An evaluated axis
+    costs 11 coordinates (a multiply and an FMA, one more off the unit cube), 11 factors and
+    5 pair sums; a step of the set-sum recurrence 8 FMAs and 9 multiplies; a region's tail
+    40 rule-sum FMAs and 5 multiplies, the fourth differences (5 d + 1, and the products of
+    their point values), 27 null-rule FMAs and 27 multiplies, and 10 more (volume, error
+    ladder, results).  A region alone evaluates d axes and d steps.  A sibling pair
+    evaluates d + 1 axes (the second sibling's split axis only) and d + 1 steps (d - 1
+    shared); a pair whose parent's terms are kept evaluates the split axis of each sibling
+    and adds 2 sums for every other axis.  `paired`: the share of regions evaluated in
+    pairs; `cached`: the share of pairs with their parent's terms."""
+    axis = 11 * (2 if unit else 3) + 11 * _factor_ops(family) + 5
+    step = 8 + 9
+    tail = 45 + (5 * d + 1) + _fd_products(d) + 54 + (d - 1) + 10
+    alone = d * (axis + step) + tail
+    pair = (d + 1) * axis + (d + 1) * step + 2 * tail
+    pair_cached = 2 * axis + 2 * (d - 1) + (d + 1) * step + 2 * tail
+    per_pair = (1.0 - cached) * pair + cached * pair_cached
+    return (1.0 - paired) * alone + paired * per_pair / 2
 
 
 def points_ops(family, d, unit=True):
@@ -422,11 +452,19 @@ def roofline(ctx, cases, results, st, steps, mode):
     """Roofline of the dominant kernel (region evaluation, FP64 pipe)."""
     import gpuintegration_gb300 as pg
     sep = (pg.PRODUCT_PEAK, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.PRODUCT)
+    # Every region after an integral's first split is evaluated with its
+    # sibling; the share of pairs with kept parent terms is the run's.
+    cached = st.setsum_cached_pairs / max(st.setsum_pairs, 1)
     ops = 0.0
     for c, r in zip(cases, results):
         f = c.integrand
         regions = r.neval // _feval(f.ndim)
-        per = setsum_ops(f.family, f.ndim) if (mode == 1 and f.family in sep) else points_ops(f.family, f.ndim)
+        if mode == 1 and f.family in sep:
+            first = _first_split(f.ndim)
+            paired = max(regions - first, 0) / max(regions, 1)
+            per = setsum_ops(f.family, f.ndim, paired=paired, cached=cached)
+        else:
+            per = points_ops(f.family, f.ndim)
         ops += regions * per
     ops *= steps
     eval_s = st.eval_ms / 1000.0

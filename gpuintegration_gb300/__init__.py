@@ -78,7 +78,8 @@ class PgStats(ctypes.Structure):
                 ("eval_bytes", ctypes.c_uint64), ("host_ms", ctypes.c_double), ("sync_ms", ctypes.c_double),
                 ("spill_ms", ctypes.c_double), ("admit_ms", ctypes.c_double),
                 ("setsum_regions", ctypes.c_uint64), ("classify_ms", ctypes.c_double),
-                ("classify_passes", ctypes.c_uint64)]
+                ("classify_passes", ctypes.c_uint64), ("setsum_pairs", ctypes.c_uint64),
+                ("setsum_cached_pairs", ctypes.c_uint64)]
 
 
 class PgIterationRecord(ctypes.Structure):
@@ -122,6 +123,7 @@ def load_library(path: str = LIB_PATH):
         "pg_context_reset_stats": (ctypes.c_int, [c_ctx]),
         "pg_context_iterations": (ctypes.c_int, [c_ctx, P(PgIterationRecord), ctypes.c_uint64,
                                                  P(ctypes.c_uint64)]),
+        "pg_context_fail_allocation": (ctypes.c_int, [c_ctx, ctypes.c_int64]),
         "pg_context_stream": (ctypes.c_void_p, [c_ctx]),
         "pg_synchronize": (ctypes.c_int, [c_ctx]),
         "pg_integrate_regions": (ctypes.c_int, [c_ctx, P(PgIntegrand), _D, _D, ctypes.c_uint64, ctypes.c_double,
@@ -288,6 +290,10 @@ class Context:
 
     def reset_stats(self):
         self.lib.pg_context_reset_stats(self.h)
+
+    def fail_allocation(self, after: int):
+        """Testing hook: the allocation after `after` more fails with PG_OOM (negative: off)."""
+        self._check(self.lib.pg_context_fail_allocation(self.h, int(after)), allow=(PG_OK,))
 
     def iterations(self) -> np.ndarray:
         """Per-iteration records since the last reset_stats (profiling on): a structured

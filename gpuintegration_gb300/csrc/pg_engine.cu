@@ -148,6 +148,7 @@ Engine::~Engine() {
   cudaSetDevice(device);
   DevBuf* dev_bufs[] = {&rule_trie_, &rule_leafset_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
                         &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
+                        &terms_, &cache_,
                         &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
                         &thr_out_, &thr_counts_, &adm_starts_, &adm_ids_, &rst_items_};
   for (DevBuf* b : dev_bufs)
@@ -243,6 +244,7 @@ int Engine::ensure(DevBuf& b, size_t bytes) {
   b.p = nullptr;
   b.bytes = 0;
   size_t want = std::max(bytes, (size_t)4096);
+  if (fail_alloc_after >= 0 && fail_alloc_after-- == 0) return fail(cudaErrorMemoryAllocation, "cudaMalloc (injected)");
   PG_TRY(cudaMalloc(&b.p, want), "cudaMalloc");
   b.bytes = want;
   return PG_OK;
@@ -255,6 +257,8 @@ int Engine::ensure_pinned(DevBuf& b, size_t bytes) {
   b.p = nullptr;
   b.bytes = 0;
   size_t want = std::max(bytes, (size_t)4096);
+  if (fail_alloc_after >= 0 && fail_alloc_after-- == 0)
+    return fail(cudaErrorMemoryAllocation, "cudaMallocHost (injected)");
   PG_TRY(cudaMallocHost(&b.p, want), "cudaMallocHost");
   b.bytes = want;
   return PG_OK;
@@ -367,6 +371,7 @@ int Engine::evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left,
   EvalLaunch L{d_left, d_length, n, stride, nullptr, (const IntegralDesc*)descs_.p, &rule_, d_est, d_err, d_bisect,
                desc.d, num_sms, stream_, tn.warps, tn.ctas_per_sm};
   L.mode = (mode == PG_EVAL_SET_SUMS && family_separable(desc.family)) ? PG_EVAL_SET_SUMS : PG_EVAL_POINTS;
+  L.scale = desc.jac != 1.0;
   if (profiling) cudaEventRecord(ev_[0], stream_);
   PG_TRY(launch(L), "evaluation launch");
   stats.launches++;
@@ -603,7 +608,8 @@ int Engine::grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_
 }
 
 int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
-                    uint64_t out_stride, uint32_t* out_owner, double* parent_out) {
+                    uint64_t out_stride, uint32_t* out_owner, double* parent_out, const double* terms,
+                    int terms_rows, double* cache_out, int cache_rows) {
   (void)nxt;
   if (nchunks == 0) return PG_OK;
   if (maxd <= 8) {
@@ -611,13 +617,15 @@ int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int max
         (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
         (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
         (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
-        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0);
+        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0, terms, terms_rows,
+        cache_out, cache_rows);
   } else {
     compact_split_kernel<16><<<nchunks, kRedThreads, 0, stream_>>>(
         (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
         (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
         (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
-        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0);
+        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0, terms, terms_rows,
+        cache_out, cache_rows);
   }
   stats.launches++;
   PG_TRY(cudaGetLastError(), "compact/split launch");
@@ -632,6 +640,7 @@ int Engine::evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& l
   struct Run {
     uint64_t start, n;
     int mode, maxd;
+    bool scale;
   };
   std::vector<uint32_t> order(live);
   std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return jobs[a].start < jobs[b].start; });
@@ -640,11 +649,13 @@ int Engine::evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& l
     const Job& J = jobs[j];
     if (J.n == 0) continue;
     const int md = job_eval_mode(J);
+    const bool sc = J.desc.jac != 1.0;
     if (!runs.empty() && runs.back().mode == md && runs.back().start + runs.back().n == J.start) {
       runs.back().n += J.n;
       runs.back().maxd = std::max(runs.back().maxd, J.desc.d);
+      runs.back().scale |= sc;
     } else {
-      runs.push_back(Run{J.start, J.n, md, J.desc.d});
+      runs.push_back(Run{J.start, J.n, md, J.desc.d, sc});
     }
   }
   const double* left = (const double*)left_[cur].p;
@@ -662,6 +673,13 @@ int Engine::evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& l
     L.mode = R.mode;
     L.segs = (const SegDesc*)segs_.p;
     L.base = R.start;
+    L.scale = R.scale;
+    if (R.mode == PG_EVAL_SET_SUMS && terms_rows_ > 0) {
+      L.pcache = cache_.p ? (const double*)cache_.p : nullptr;
+      L.pcache_rows = terms_rows_ + 1;
+      L.terms = (double*)terms_.p;
+      L.terms_rows = terms_rows_;
+    }
     PG_TRY(launch(L), "evaluation launch");
     stats.launches++;
     stats.eval_launches++;
@@ -677,10 +695,20 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   const uint32_t njobs = (uint32_t)jobs.size();
   if (njobs == 0) return PG_OK;
   int maxd = 2;
-  for (auto& J : jobs) maxd = std::max(maxd, J.desc.d);
+  bool use_cache = false;  // keep the bisected regions' per-axis terms for the set-sum kernel
+  for (auto& J : jobs) {
+    maxd = std::max(maxd, J.desc.d);
+    use_cache |= job_eval_mode(J) == PG_EVAL_SET_SUMS;
+  }
+  {
+    const char* env = std::getenv("PG_SETSUM_CACHE");
+    if (env && env[0] == '0') use_cache = false;
+  }
+  const int term_rows = kTermValues * maxd;  // + one row for the split axis in the parents' cache
   // Pool capacity in regions: both region lists, owners, parents and the
-  // per-region scratch of one iteration.
-  const uint64_t bytes_per_region = 32ull * maxd + 53;
+  // per-region scratch of one iteration (with the kept terms: this list's and
+  // its parents', half as many).
+  const uint64_t bytes_per_region = 32ull * maxd + 53 + (use_cache ? 8ull * term_rows + 4ull * (term_rows + 1) : 0);
   uint64_t cap = policy.max_regions;
   if (cap == 0) {
     size_t fr = 0, tot = 0;
@@ -727,6 +755,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     J.n = J.init_n ? J.init_n : ipow_u((uint64_t)parts_for(J.desc.d), J.desc.d);
     J.start = J.par_start = 0;
     J.has_parent = 0;
+    J.has_cache = 0;
     J.iters = 0;
     J.done = false;
     J.state = JOB_PENDING;
@@ -800,6 +829,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
             adm_pending.push_back(j);
           }
           J.state = JOB_RESIDENT;
+          J.has_cache = 0;
         }
       if (t > T) {
         if ((rc = grow_list(cur, t, maxd, T, P)) != PG_OK) return rc;
@@ -917,11 +947,16 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       S.chunk_start = (uint32_t)chunk_list.size();
       S.nchunks = (uint32_t)div_up(S.n, kChunk);
       S.has_parent = J.has_parent;
+      S.has_cache = J.has_cache;
       // predict_split (Workspace.cuh:415-420): no rel-err classification while
       // the list is small, in the first 15 iterations, and nothing finished yet.
       S.relerr = J.opt.predict_split ? !(J.n <= 15000000ull && J.iters < 15 && J.res.nregions == 0)
                                      : J.opt.relerr_classification;
       S.epsrel = J.epsrel;
+      if (res && S.has_parent && S.n > 0 && (S.n & 1ull) == 0 && job_eval_mode(J) == PG_EVAL_SET_SUMS) {
+        stats.setsum_pairs += S.n / 2;  // the set-sum kernel's sibling pairing
+        if (S.has_cache) stats.setsum_cached_pairs += S.n / 2;
+      }
       for (uint32_t b = 0; b < S.nchunks; ++b) chunk_list.push_back(ChunkRef{j, b});
       hs[j] = S;
     }
@@ -932,6 +967,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     if ((rc = ensure(err_b_, N * 8)) != PG_OK) return rc;
     if ((rc = ensure(bisect_, N * 4)) != PG_OK) return rc;
     if ((rc = ensure(active_, N)) != PG_OK) return rc;
+    terms_rows_ = use_cache ? term_rows : 0;
+    if (use_cache && (rc = ensure(terms_, div_up(N, 32) * 256 * (uint64_t)term_rows)) != PG_OK) return rc;
     if ((rc = ensure(partials_, nchunks * sizeof(Partial))) != PG_OK) return rc;
     if ((rc = ensure(chunk_off_, nchunks * 8)) != PG_OK) return rc;
     if ((rc = ensure(chunks_, nchunks * sizeof(ChunkRef))) != PG_OK) return rc;
@@ -954,8 +991,14 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     if ((rc = evaluate_list(jobs, live, cur, N, launch)) != PG_OK) return rc;
     stats.regions_evaluated += N;
     for (uint32_t j : live) {
-      stats.points_evaluated += jobs[j].n * (uint64_t)rule_.feval[jobs[j].desc.d];
-      stats.eval_bytes += jobs[j].n * (16ull * jobs[j].desc.d + 24ull);  // + the 4-byte owner of a shared list
+      const Job& J = jobs[j];
+      const uint64_t d = (uint64_t)J.desc.d;
+      stats.points_evaluated += J.n * (uint64_t)rule_.feval[J.desc.d];
+      stats.eval_bytes += J.n * (16ull * d + 24ull);  // + the 4-byte owner of a shared list
+      if (use_cache && job_eval_mode(J) == PG_EVAL_SET_SUMS) {
+        stats.eval_bytes += J.n * 8ull * kTermValues * d;  // the terms written
+        if (J.has_cache) stats.eval_bytes += (J.n / 2) * (8ull * kTermValues * (d - 1) + 8ull);  // parents' read
+      }
     }
     if (profiling) cudaEventRecord(ev_[1], stream_);
     // 2. two-level error + classification + partial sums; 3. per-integral totals
@@ -1105,6 +1148,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
         Transition& Tr = ht[j];
         Tr.mode = mode[j];
         Tr.A = keepA[j];
+        Tr.cache = use_cache && job_eval_mode(J) == PG_EVAL_SET_SUMS;
         if (out_total + 2 * keepA[j] <= cap || out_total == 0) {
           Tr.out_start = out_total;
           Tr.par_out = par_total;
@@ -1191,6 +1235,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
           J.state = JOB_SPILLED;
           J.n = 2 * keepA[spill[q]];
           J.has_parent = 1;
+          J.has_cache = 0;
         }
       }
       PG_TRY(cudaMemcpyAsync(trans_.p, ht, njobs * sizeof(Transition), cudaMemcpyHostToDevice, stream_),
@@ -1205,9 +1250,15 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     const int nxt = cur ^ 1;
     if (out_total > 0) {
       if ((rc = grow_list(nxt, out_total, maxd, 0, 0)) != PG_OK) return rc;
+      // This iteration's evaluation has read the parents' terms; the cache now
+      // takes the terms of the regions being bisected.
+      if (use_cache && (rc = ensure(cache_, div_up(par_total, 32) * 256 * (uint64_t)(term_rows + 1))) != PG_OK)
+        return rc;
       if (profiling) cudaEventRecord(ev_[4], stream_);
       if ((rc = compact(cur, nxt, 0, (uint32_t)nchunks, maxd, (double*)left_[nxt].p, (double*)len_[nxt].p,
-                        reg_cap_[nxt], (uint32_t*)owner_[nxt].p, (double*)parent_[nxt].p)) != PG_OK)
+                        reg_cap_[nxt], (uint32_t*)owner_[nxt].p, (double*)parent_[nxt].p,
+                        use_cache ? (const double*)terms_.p : nullptr, term_rows,
+                        use_cache ? (double*)cache_.p : nullptr, term_rows + 1)) != PG_OK)
         return rc;
       if (profiling) {
         cudaEventRecord(ev_[5], stream_);
@@ -1220,10 +1271,12 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       if (J.state != JOB_RESIDENT || Tr.mode == 0) continue;
       stats.stage_bytes += J.n + Tr.A * (uint64_t)(16 * J.desc.d + 12) + 2 * Tr.A * (uint64_t)(16 * J.desc.d + 4) +
                            Tr.A * 8;
+      if (Tr.cache) stats.stage_bytes += Tr.A * (uint64_t)(16 * kTermValues * J.desc.d + 8);  // terms kept
       J.start = Tr.out_start;
       J.n = 2 * Tr.A;
       J.par_start = Tr.par_out;
       J.has_parent = 1;
+      J.has_cache = Tr.cache;
     }
     T = out_total;
     P = par_total;
@@ -1313,7 +1366,15 @@ int Engine::autotune() {
 // ---------------------------------------------------------------------------
 cudaError_t launch_family_eval(const EvalLaunch& L) {
   const pg_eval_args a = eval_args_of(L);
-  if (L.mode == PG_EVAL_SET_SUMS) return launch_setsum(a, L.segs, L.base);
+  if (L.mode == PG_EVAL_SET_SUMS) {
+    SetSumCache c;
+    c.pcache = L.pcache;
+    c.pcache_rows = L.pcache_rows;
+    c.terms = L.terms;
+    c.terms_rows = L.terms_rows;
+    c.scale = L.scale;
+    return launch_setsum(a, L.segs, L.base, c);
+  }
   return L.maxd <= 8 ? launch_eval<8>(a, FamilyFn{}) : launch_eval<16>(a, FamilyFn{});
 }
 

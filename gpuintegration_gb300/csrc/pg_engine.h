@@ -44,6 +44,13 @@ struct EvalLaunch {
   // left[0].
   const SegDesc* segs = nullptr;
   uint64_t base = 0;
+  // Set-sum kernel only: the parents' kept terms and this list's terms
+  // (null: none kept / none written).
+  const double* pcache = nullptr;
+  int pcache_rows = 0;
+  double* terms = nullptr;
+  int terms_rows = 0;
+  bool scale = true;  // some integral of the launch has a Jacobian other than 1
 };
 
 // Launch shape of the evaluation kernel for one kernel class (d <= 8, d > 8),
@@ -113,6 +120,7 @@ struct Job {
   uint64_t start = 0;  // first region in the current list
   uint64_t par_start = 0;
   int has_parent = 0;
+  int has_cache = 0;  // its parents' per-axis terms are in the engine's parent cache
   int iters = 0;
   bool done = false;
   int error = 0;
@@ -220,6 +228,9 @@ class Engine {
   std::vector<pg_iteration_record> iterations;  // while profiling
   bool profiling = false;
   std::string last_error;
+  // Allocation-failure hook (pg_context_fail_allocation): the allocation after
+  // this many more fails as an out-of-memory cudaMalloc would; -1: off.
+  int64_t fail_alloc_after = -1;
   int device = 0;
   int num_sms = 152;
 
@@ -236,7 +247,8 @@ class Engine {
   int threshold_counts(uint32_t jidx, const double* thr, int k, uint64_t* counts);
   int grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_t live_par);
   int compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
-              uint64_t out_stride, uint32_t* out_owner, double* parent_out);
+              uint64_t out_stride, uint32_t* out_owner, double* parent_out, const double* terms = nullptr,
+              int terms_rows = 0, double* cache_out = nullptr, int cache_rows = 0);
   // Launches the evaluation of list `cur`'s regions [0, N): one launch per
   // maximal range of resident integrals that share an evaluation kernel.
   int evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& live, int cur, uint64_t N,
@@ -252,6 +264,11 @@ class Engine {
   int reg_rows_[2] = {0, 0};
   // per-region scratch
   DevBuf est_, err_a_, err_b_, bisect_, active_;
+  // set-sum evaluation: this list's per-axis terms (tiles of terms_rows_ rows
+  // by list position) and the kept parents' (tiles of terms_rows_ + 1 rows by
+  // parent index; the extra row holds the split axis)
+  DevBuf terms_, cache_;
+  int terms_rows_ = 0;
   // per-chunk
   DevBuf partials_, chunk_off_, chunks_;
   // per-integral

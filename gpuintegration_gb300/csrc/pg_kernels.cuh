@@ -24,6 +24,19 @@
 
 namespace pg {
 
+// Per-axis values of a region that the set-sum evaluation keeps for its
+// children: the factor at the centre, at +-G0 and +-G1, and the sums p2..p4.
+constexpr int kTermValues = 8;
+
+// Term buffers are tiled by 32 consecutive positions: value `row` of position
+// `pos` sits at ((pos / 32) * rows + row) * 32 + pos % 32, so a warp's values
+// share one block of rows * 256 bytes (a plain row-major layout puts each row
+// a list's length apart, and a warp touching a hundred rows spreads over a
+// hundred pages).
+__host__ __device__ __forceinline__ uint64_t term_at(uint64_t pos, int row, int rows) {
+  return ((pos >> 5) * (uint64_t)rows + (uint64_t)row) * 32ull + (pos & 31ull);
+}
+
 // Segment of one integral in the current region list.
 struct SegDesc {
   uint64_t start;      // first region
@@ -34,6 +47,8 @@ struct SegDesc {
   int32_t has_parent;
   int32_t relerr;
   double epsrel;
+  int32_t has_cache;  // the parents' per-axis terms are kept (set-sum evaluation of sibling pairs)
+  int32_t pad;
 };
 
 struct ChunkRef {
@@ -63,7 +78,7 @@ struct Transition {
   uint64_t A;          // kept regions (children: 2A)
   uint64_t par_out;    // first parent estimate written for the next iteration
   int32_t mode;        // 0 drop, 1 keep the flagged regions, 2 keep every region
-  int32_t pad;
+  int32_t cache;       // 1: keep the kept regions' per-axis terms for their children
 };
 
 // ---------------------------------------------------------------------------
@@ -225,7 +240,9 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
                          const double* __restrict__ left, const double* __restrict__ length, uint64_t stride,
                          const int32_t* __restrict__ bisect, const double* __restrict__ est,
                          double* __restrict__ out_left, double* __restrict__ out_length, uint64_t out_stride,
-                         uint32_t* __restrict__ out_owner, double* __restrict__ parent_out, uint32_t chunk0) {
+                         uint32_t* __restrict__ out_owner, double* __restrict__ parent_out, uint32_t chunk0,
+                         const double* __restrict__ terms, int terms_rows, double* __restrict__ cache_out,
+                         int cache_rows) {
   __shared__ uint32_t wcount[kRedThreads / 32];
   const uint32_t cidx = chunk0 + blockIdx.x;
   const ChunkRef cr = chunks[cidx];
@@ -288,6 +305,15 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
         out_owner[c1] = cr.integral;
       }
       parent_out[T.par_out + pos] = e;
+      if (cache_out && T.cache) {
+        // The region's per-axis terms for its children, and the axis it is
+        // split on (the one axis whose terms the children evaluate).
+        const int rows = kTermValues * d;
+        const uint64_t pj = T.par_out + pos;
+#pragma unroll 4
+        for (int q = 0; q < rows; ++q) cache_out[term_at(pj, q, cache_rows)] = terms[term_at(i, q, terms_rows)];
+        cache_out[term_at(pj, rows, cache_rows)] = (double)bd;
+      }
     }
     run += total;
     __syncthreads();  // wcount is rewritten by the next slice

@@ -45,6 +45,15 @@
 // (Sample.cuh:190-290, Phases.cuh:329-348) with the same operations as
 // eval_kernel.
 //
+// Parent terms: a region's eight values per axis (c, h(+G0), h(-G0),
+// h(+G1), h(-G1), p2, p3, p4; p0 and p1 are sums of the second to fifth) are
+// written to `terms`, and the compaction keeps those of the regions it
+// bisects, with the split axis in one more row.  Both children of a region
+// share its coordinates on every axis but the split one, so a pair whose
+// parent's values are kept takes them from there and evaluates only the split
+// axis's factors: 22 per pair instead of 99 at d = 8.  The values are those
+// the children would compute, bit for bit.
+//
 // One thread per region or sibling pair: with a thread per region every FP64
 // warp instruction carries 32 regions' work, and the SoA loads of the bounds
 // and the stores of the results are coalesced across the warp.
@@ -58,12 +67,19 @@
 
 namespace pg {
 
-// Multiply of the set-sum kernel: the IEEE product on the integer pipe.
+// Multiplies of the set-sum kernel: on the FP64 pipe (__dmul_rn), or with
+// -DPG_SETSUM_MUL=mul_rn_int on the integer pipe; the same bits either way.
+// (With the parents' terms kept, the FP64 pipe has room for them: on GB300
+// the FP64 form is 10-18% faster on 8-D integrals and as fast on the batched
+// workload.)
 #ifndef PG_SETSUM_MUL
-#define PG_SETSUM_MUL mul_rn_int
+#define PG_SETSUM_MUL __dmul_rn
 #endif
 
 constexpr int kSetSumThreads = 128;
+#ifndef PG_SETSUM_MIN_BLOCKS
+#define PG_SETSUM_MIN_BLOCKS 4  // resident blocks per SM the register allocation allows
+#endif
 constexpr int kFdValues = 5;  // per axis: factor at the centre, +G0, -G0, +G1, -G1
 
 template <int MAXD>
@@ -115,15 +131,43 @@ __device__ __forceinline__ AxisTerm axis_term(const IntegralDesc& D, const RuleD
                   __dadd_rn(h[5], h[10])};
 }
 
+// Writes one axis's terms (the five values at fd[v * T] and p2..p4) for the
+// region at list position pos.
+__device__ __forceinline__ void put_terms(double* __restrict__ terms, int rows, uint64_t pos, int k,
+                                          const double* fd, int T, const AxisTerm& A) {
+  double* t = terms + term_at(pos, k * kTermValues, rows);
+#pragma unroll
+  for (int v = 0; v < kFdValues; ++v) t[v * 32] = fd[v * T];
+  t[5 * 32] = A.p2;
+  t[6 * 32] = A.p3;
+  t[7 * 32] = A.p4;
+}
+
+// One axis's terms of a parent, kept at parent index pidx; the five values the
+// fourth differences read go to fd[v * T].
+__device__ __forceinline__ AxisTerm cached_term(const double* __restrict__ cache, int rows, uint64_t pidx, int k,
+                                                double* fd, int T) {
+  const double* t = cache + term_at(pidx, k * kTermValues, rows);
+  double v[kTermValues];
+#pragma unroll
+  for (int q = 0; q < kTermValues; ++q) v[q] = t[q * 32];
+#pragma unroll
+  for (int q = 0; q < kFdValues; ++q) fd[q * T] = v[q];
+  return AxisTerm{v[0], __dadd_rn(v[1], v[2]), __dadd_rn(v[3], v[4]), v[5], v[6], v[7]};
+}
+
 // Rule sums, split axis and null-rule error of one region from its set sums.
 // Factor value v of axis k is fv[(k * 5 + v) * T], except on axis `sk`, whose
 // values are at own[v * T].
-template <int MAXD>
+template <int MAXD, bool SCALE>
 __device__ __forceinline__ void region_result(const SetSumSmem<MAXD>& Sm, const RuleDev& rule, const SetSums& Q,
                                               int d, double jac, double vol, int maxdim, const double* fv, int sk,
                                               const double* own, double* est, double* err, int32_t* bisect) {
   constexpr int T = kSetSumThreads;
-  const bool scale_jac = jac != 1.0;
+  // Jacobian scaling (a box other than the unit cube): compiled out of
+  // launches whose integrals all have jac = 1, where a predicated multiply
+  // would still run.
+  const bool scale_jac = SCALE && jac != 1.0;
   const double* W = Sm.w + d * 45;
   double s5[kNRules];
 #pragma unroll
@@ -190,18 +234,18 @@ __device__ __forceinline__ void region_result(const SetSumSmem<MAXD>& Sm, const 
   // their bit patterns, a NaN term ignored.
   const double* SC = Sm.scale + d * 45;
   const double* NM = Sm.norm + d * 45;
+  // (A maximum of bit patterns does not depend on the order of its terms; one
+  // generator set at a time keeps few products live.)
   unsigned long long mq[3] = {0ull, 0ull, 0ull};
+#pragma unroll 1
+  for (int st = 0; st < kNSets; ++st) {
 #pragma unroll
-  for (int q = 1; q <= 3; ++q) {
-    unsigned long long mx = 0ull;
-#pragma unroll
-    for (int st = 0; st < kNSets; ++st) {
+    for (int q = 1; q <= 3; ++q) {
       const unsigned long long bt = (unsigned long long)__double_as_longlong(
           PG_SETSUM_MUL(fabs(__fma_rn(SC[st * kNRules + q], s5[q], s5[q + 1])), NM[st * kNRules + q]));
       const unsigned long long term = (bt & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : bt;
-      mx = term > mx ? term : mx;
+      mq[q - 1] = term > mq[q - 1] ? term : mq[q - 1];
     }
-    mq[q - 1] = mx;
   }
   const double e1 = __longlong_as_double((long long)mq[0]), e2 = __longlong_as_double((long long)mq[1]),
                e3 = __longlong_as_double((long long)mq[2]);
@@ -227,19 +271,24 @@ __device__ __forceinline__ void side_step(int k, double side, double& vol, unsig
 }
 
 // Regions [0, n) of a run that starts at list position `base`, one per
-// thread, blocks in list order.  (A grid-stride loop over tens of millions of
-// regions lets the blocks drift apart over the list, and the scattered loads
+// thread, blocks in list order.  With `terms` (tiles of `terms_rows` rows,
+// by list position) every region's terms are written; with `pcache` (tiles of
+// `pcache_rows` rows, by parent index) pairs of segments flagged has_cache
+// take their shared axes' terms from their parent.
+// (A grid-stride loop over tens of millions of regions lets the blocks drift
+// apart over the list, and the scattered loads
 // of the SoA rows made each region up to 40% dearer.)  With `segs` (the
 // integrals' segments of the list), a region in the first half of a segment
 // that has a parent level is evaluated together with its sibling in the
 // second half, and second-half regions are left to their sibling's thread;
 // without, every region is evaluated alone.
-template <int MAXD>
-static __global__ void __launch_bounds__(kSetSumThreads, 4)
+template <int MAXD, bool SCALE>
+static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
     setsum_kernel(const double* __restrict__ left, const double* __restrict__ length, uint64_t n, uint64_t stride,
                   const uint32_t* __restrict__ owner, const IntegralDesc* __restrict__ descs, RuleDev rule,
                   double* __restrict__ est, double* __restrict__ err, int32_t* __restrict__ bisect,
-                  const SegDesc* __restrict__ segs, uint64_t base) {
+                  const SegDesc* __restrict__ segs, uint64_t base, const double* __restrict__ pcache,
+                  int pcache_rows, double* __restrict__ terms, int terms_rows) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SetSumSmem<MAXD>& Sm = *reinterpret_cast<SetSumSmem<MAXD>*>(smem_raw);
   constexpr int T = kSetSumThreads;
@@ -247,6 +296,8 @@ static __global__ void __launch_bounds__(kSetSumThreads, 4)
   bool work = r < n;
   uint32_t j = 0;
   uint64_t rb = r;  // the sibling evaluated with r (r itself: none)
+  bool cached = false;
+  uint64_t pidx = 0;  // the pair's parent index
   if (work) {
     j = owner ? owner[r] : 0u;
     if (segs) {
@@ -256,6 +307,8 @@ static __global__ void __launch_bounds__(kSetSumThreads, 4)
         if (local >= half) work = false;  // evaluated with its sibling
         rb = r + half;
         if (rb >= n) rb = r;  // a segment always lies inside one run; never read outside it
+        cached = pcache && S.has_cache && rb != r;
+        pidx = S.par_start + local;
       }
     }
   }
@@ -273,9 +326,14 @@ static __global__ void __launch_bounds__(kSetSumThreads, 4)
   const IntegralDesc& D = descs[j];
   const int d = D.d;
   const bool unit = D.unit != 0;
-  // The deferred axis: the one the siblings differ on, else the last.
+  // The deferred axis: the parent's split axis when its terms are kept, else
+  // the one the siblings differ on, else the last.  (Siblings whose lower
+  // bounds coincide, when half the parent's side is below the bound's
+  // rounding, still differ from the parent on the split axis.)
   int s = d - 1;
-  if (pair)
+  if (cached)
+    s = min(max((int)pcache[term_at(pidx, kTermValues * d, pcache_rows)], 0), d - 1);
+  else if (pair)
     for (int k = d - 1; k >= 0; --k)
       if (left[(uint64_t)k * stride + r] != left[(uint64_t)k * stride + rb]) s = k;
   SetSums Q{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0};
@@ -292,51 +350,86 @@ static __global__ void __launch_bounds__(kSetSumThreads, 4)
     sideb = __dsub_rn(up, lo);
     Bs = axis_term(D, rule, s, lo, up, unit, fvb, T);
   }
+  // With the parent's terms, the pair's own factors on the split axis come
+  // first: every thread of the warp evaluates one axis here, whichever it is,
+  // and the loop below only loads.  (Evaluated inside the loop at k == s, the
+  // lanes' different split axes would make the warp run the factors at
+  // nearly every k.)
+  AxisTerm Ac{};
+  if (cached) {
+    const double lo = left[(uint64_t)s * stride + r];
+    const double up = __dadd_rn(lo, length[(uint64_t)s * stride + r]);
+    Ac = axis_term(D, rule, s, lo, up, unit, fv + (s * kFdValues) * T, T);
+  }
   for (int k = 0; k < d; ++k) {
     const double lo = left[(uint64_t)k * stride + r];
     const double up = __dadd_rn(lo, length[(uint64_t)k * stride + r]);
     const double side = __dsub_rn(up, lo);
     side_step(k, side, vol, widest, maxdim);
     if (pair) side_step(k, k == s ? sideb : side, volb, widestb, maxdimb);
-    const AxisTerm A = axis_term(D, rule, k, lo, up, unit, fv + (k * kFdValues) * T, T);
+    double* const fk = fv + (k * kFdValues) * T;
+    AxisTerm A;
+    if (cached)
+      A = (k == s) ? Ac : cached_term(pcache, pcache_rows, pidx, k, fk, T);
+    else
+      A = axis_term(D, rule, k, lo, up, unit, fk, T);
+    if (terms) {
+      put_terms(terms, terms_rows, base + r, k, fk, T, A);
+      if (pair && k != s) put_terms(terms, terms_rows, base + rb, k, fk, T, A);
+    }
     if (k == s)
       As = A;
     else
       set_step(Q, A);
   }
+  if (pair && terms) put_terms(terms, terms_rows, base + rb, s, fvb, T, Bs);
   const double jac = D.jac;
   {
     SetSums R = Q;
     set_step(R, As);
-    region_result<MAXD>(Sm, rule, R, d, jac, vol, maxdim, fv, -1, fv, &est[r], &err[r], &bisect[r]);
+    region_result<MAXD, SCALE>(Sm, rule, R, d, jac, vol, maxdim, fv, -1, fv, &est[r], &err[r], &bisect[r]);
   }
   if (pair) {
     SetSums R = Q;
     set_step(R, Bs);
-    region_result<MAXD>(Sm, rule, R, d, jac, volb, maxdimb, fv, s, fvb, &est[rb], &err[rb], &bisect[rb]);
+    region_result<MAXD, SCALE>(Sm, rule, R, d, jac, volb, maxdimb, fv, s, fvb, &est[rb], &err[rb], &bisect[rb]);
   }
 }
 
 // Launch of the set-sum kernel over a run of the region list whose integrals
 // all have product-form families: one thread per region.  `segs` may be null
 // (no sibling pairing); `base` is the run's first list position.
-template <int MAXD>
-inline cudaError_t launch_setsum_shape(const pg_eval_args& a, const SegDesc* segs, uint64_t base) {
+struct SetSumCache {
+  const double* pcache = nullptr;  // parents' terms, row k * 8 + v of tiles by parent index
+  int pcache_rows = 0;             // rows per tile (8 * the list's largest dimension + 1)
+  double* terms = nullptr;         // this list's terms, row k * 8 + v of tiles by list position
+  int terms_rows = 0;              // rows per tile (8 * the list's largest dimension)
+  bool scale = true;               // some integral of the run has a box other than the unit cube
+};
+
+template <int MAXD, bool SCALE>
+inline cudaError_t launch_setsum_shape(const pg_eval_args& a, const SegDesc* segs, uint64_t base,
+                                       const SetSumCache& c) {
   const size_t smem = sizeof(SetSumSmem<MAXD>);
   static std::atomic<unsigned long long> attr_done{0};
-  const cudaError_t ae = ensure_dynamic_smem(setsum_kernel<MAXD>, (int)smem, attr_done);
+  const cudaError_t ae = ensure_dynamic_smem(setsum_kernel<MAXD, SCALE>, (int)smem, attr_done);
   if (ae != cudaSuccess) return ae;
   if (a.n == 0) return cudaSuccess;
   const uint64_t g = (a.n + kSetSumThreads - 1) / kSetSumThreads;
   if (g > 0x7fffffffull) return cudaErrorInvalidValue;
-  setsum_kernel<MAXD><<<(unsigned)g, kSetSumThreads, smem, (cudaStream_t)a.stream>>>(
+  setsum_kernel<MAXD, SCALE><<<(unsigned)g, kSetSumThreads, smem, (cudaStream_t)a.stream>>>(
       a.left, a.length, a.n, a.stride, a.owner, static_cast<const IntegralDesc*>(a.descs),
-      *static_cast<const RuleDev*>(a.rule), a.est, a.err, a.bisect, segs, base);
+      *static_cast<const RuleDev*>(a.rule), a.est, a.err, a.bisect, segs, base, c.pcache, c.pcache_rows, c.terms,
+      c.terms_rows);
   return cudaGetLastError();
 }
 
-inline cudaError_t launch_setsum(const pg_eval_args& a, const SegDesc* segs, uint64_t base) {
-  return a.maxd <= 8 ? launch_setsum_shape<8>(a, segs, base) : launch_setsum_shape<kMaxNdim>(a, segs, base);
+inline cudaError_t launch_setsum(const pg_eval_args& a, const SegDesc* segs, uint64_t base,
+                                 const SetSumCache& c = SetSumCache()) {
+  if (a.maxd <= 8)
+    return c.scale ? launch_setsum_shape<8, true>(a, segs, base, c) : launch_setsum_shape<8, false>(a, segs, base, c);
+  return c.scale ? launch_setsum_shape<kMaxNdim, true>(a, segs, base, c)
+                 : launch_setsum_shape<kMaxNdim, false>(a, segs, base, c);
 }
 
 }  // namespace pg

@@ -151,6 +151,8 @@ typedef struct pg_stats {
   uint64_t setsum_regions;      /* regions evaluated by generator-set sums (PG_EVAL_SET_SUMS) */
   double classify_ms;           /* host time in the memory-pressure classifier (its passes included) */
   uint64_t classify_passes;     /* threshold passes of the classifier (each a launch and a readback) */
+  uint64_t setsum_pairs;        /* sibling pairs evaluated together by the set-sum kernel */
+  uint64_t setsum_cached_pairs; /* of those, pairs that took their parent's kept per-axis terms */
 } pg_stats;
 
 /* One iteration of a run (recorded while profiling is on): regions in the
@@ -180,6 +182,13 @@ int pg_context_reset_stats(pg_context* ctx);
 /* The iterations recorded since the last pg_context_reset_stats: *count
  * receives their number, out[0 .. min(count, capacity)) the records. */
 int pg_context_iterations(const pg_context* ctx, pg_iteration_record* out, uint64_t capacity, uint64_t* count);
+/* Testing hook, no counterpart in the reference: of the device and pinned
+ * host buffers this context allocates from now on, the one after `after` more
+ * fails as cudaMalloc fails when memory runs out, and the call that needed it
+ * returns PG_OOM; later allocations succeed again and the context stays
+ * usable.  after < 0 turns the hook off.  Nothing reaches the GPU: the
+ * failure is made on the host before cudaMalloc is called. */
+int pg_context_fail_allocation(pg_context* ctx, int64_t after);
 void* pg_context_stream(pg_context* ctx); /* the cudaStream_t the context launches on */
 int pg_synchronize(pg_context* ctx);
 
@@ -402,7 +411,13 @@ int pg_probe_fp64_peak(pg_context* ctx, double* tflops);
  * looks up that array's device address, so make it before any stream capture.
  * Every call uses the same array: calls whose kernels can overlap on the GPU
  * (other streams, other host threads) race, and the caller must serialise
- * them.  The result is bit-identical to pg_reduce_sum on the same data. */
+ * them.  The result is bit-identical to pg_reduce_sum on the same data.
+ * The call ends with cudaGetLastError, which also returns (and clears) an
+ * error left pending by the caller's own earlier launches, so PG_CUDA_ERROR
+ * may report an error this call did not cause.  The scratch array's device
+ * address is looked up once per device and belongs to that device's primary
+ * context: after cudaDeviceReset it is stale, and the entry point must not be
+ * called again in that process. */
 int pg_reduce_sum_noalloc(const double* d_x, uint64_t n, double* d_out, void* stream);
 
 #ifdef __cplusplus

@@ -1,10 +1,11 @@
 #!/bin/sh
 # Builds the reference-derived test programs from the reference sources where they
 # lie.  Outputs go only into oracle/_ref/ (git-ignored).  Needs the reference
-# tree (REF, default /root/reference); without it this script does nothing.
+# tree ($REF, else the directory `reference` beside this repository); without
+# it this script does nothing.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${REF:-/root/reference}
+REF=${REF:-$HERE/../../../reference}
 OUT="$HERE/../_ref"
 if [ ! -d "$REF/cuda/pagani/quad" ]; then
   echo "build_ref: reference tree not found at $REF; skipping" >&2

@@ -4,9 +4,10 @@ Candidate i is workloads.mixed_cases(..., master=4096)[i]: dim ~ U{2..8}, family
 ~ U{6 Genz}, epsrel log-uniform in [1e-7, 1e-4].  A candidate is accepted when
 PAGANI converges (status 0) and its estimate is within epsrel of the analytic
 value; the first 4096 accepted candidates form the benchmark workload.  The
-screen runs the candidates through the GPU library, whose per-integral results
-are those of the CPU oracle (bit-identical for integrands built from + - * /,
-and checked on a sample of the others by tests/test_gpu_workloads.py).
+screen runs the candidates through the GPU library's batched path, whose
+per-integral results are those of its plain path (tests/test_gpu_batch.py),
+which matches the CPU oracle (bit-identical for integrands built from
++ - * /; tests/test_gpu_parity.py, tests/test_gpu_config2.py).
 
 Writes tests/golden/config4_screen.json.  Needs a GPU.
 """

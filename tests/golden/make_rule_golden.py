@@ -1,7 +1,7 @@
 """Regenerates tests/golden/rule_tables.json from the reference itself.
 
 Builds oracle/_ref/dump_rule_tables from the reference sources (which must be
-present at $REF, default /root/reference) with oracle/ref/build_ref.sh, runs
+present at $REF, else beside this repository) with oracle/ref/build_ref.sh, runs
 it, and stores the degree-9 rule tables for ndim 2..10 with every double as a
 hex float so the comparison in tests/test_rule_tables.py is bit-exact.
 """

@@ -89,3 +89,46 @@ def test_integer_pipe_multiply_matches_fp64_multiply():
     p = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     print(p.stdout)
     assert p.returncode == 0 and p.stdout.startswith("PASS"), p.stdout + p.stderr
+
+
+def _reference_tree():
+    ref = os.environ.get("REF") or os.path.join(ROOT, "..", "reference")
+    return ref if os.path.isfile(os.path.join(ref, "common", "cuda", "Interp1D.cuh")) else None
+
+
+def test_reference_helpers_compile_in_functors():
+    """Functors built on the reference's Interp1D/2D/3D and cudaDynamicArray
+    (test/cuda/common/StatefulIntegrand.cu:34-97) compile against the C++
+    layer.  Needs the reference tree (REF); skipped without it."""
+    ref = _reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "ref_helpers_check.cu")
+    out = os.path.join(BUILD, "ref_helpers_check.o")
+    subprocess.check_call([_nvcc()] + _flags() + ["-I" + ref, "-I" + os.path.join(ref, "externals"), "-c", src,
+                                                  "-o", out])
+    assert os.path.getsize(out) > 0
+
+
+@pytest.mark.gpu
+def test_stateful_helper_functors_run(lib):
+    """Functors of the helpers' shapes (a deep-copying managed array; 1-D and
+    2-D interpolation tables) through Workspace::integrate, against their
+    exact integrals; the non-trivially-copyable functor reaches the kernel as
+    a managed copy."""
+    from gpuintegration_gb300 import _build
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "helpers_check.cu")
+    exe = os.path.join(BUILD, "helpers_check")
+    libdir = os.path.dirname(_build.LIB)
+    subprocess.check_call([_nvcc()] + _flags() + ["-cudart", "shared", src, "-L" + libdir, "-lpagani_gb300",
+                                                  "-Xlinker", "-rpath," + libdir, "-o", exe])
+    p = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    print(p.stdout)
+    lines = p.stdout.strip().splitlines()
+    assert p.returncode == 0, p.stdout + p.stderr
+    assert lines and lines[-1].startswith("DONE 0 failures")
+    names = {ln.split()[1] for ln in lines if ln.startswith("PASS")}
+    for case in ("heap_model2", "heap_model2_managed_copy", "interp1d_3", "interp2d_4"):
+        assert case in names, case

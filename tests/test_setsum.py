@@ -212,3 +212,27 @@ def test_full_loop_setsums_meet_tolerance(ctx, family):
         exact = W.analytic(f)
         assert abs(r.estimate - exact) <= 2 * eps * abs(exact) or abs(r.estimate - p.estimate) <= 1e-6 * abs(exact)
         assert abs(r.estimate - p.estimate) <= eps * abs(exact)
+
+
+@pytest.mark.gpu
+def test_parent_terms_cache_changes_no_bit(ctx, monkeypatch):
+    """Sibling pairs take the factors of every axis but the split one from
+    their parent's kept terms; those are the values they would compute, so
+    results with the cache and without it (PG_SETSUM_CACHE=0) agree bit for
+    bit, alone and in batches (with spills, whose integrals restart without
+    cached terms), at up to 12 dimensions."""
+    from gpuintegration_gb300 import workloads as W
+    rng = np.random.default_rng(31)
+    fams = (pg.GAUSSIAN, pg.C0, pg.PRODUCT_PEAK, pg.DISCONTINUOUS)
+    fs = [W.make(fams[i % 4], d, rng) for i, d in enumerate((3, 5, 8, 8, 8, 10, 12, 6))]
+    eps = [1e-4, 1e-5, 1e-4, 1e-5, 1e-6, 1e-3, 1e-3, 1e-5]
+
+    def run():
+        alone = [ctx.integrate(f, e, 0.0, options=_opts()) for f, e in zip(fs, eps)]
+        batch = ctx.batch_integrate(fs, eps, 0.0, options=_opts())
+        small = ctx.batch_integrate(fs, eps, 0.0, options=_opts(max_regions=20000))
+        return [(r.estimate, r.errorest, r.nregions, r.iters, r.status) for r in alone + batch + small]
+
+    with_cache = run()
+    monkeypatch.setenv("PG_SETSUM_CACHE", "0")
+    assert run() == with_cache
