@@ -594,13 +594,13 @@ int pg_filter_split(pg_context* ctx, int ndim, uint64_t n, const double* left, c
           (const pg::ChunkRef*)ctx->s_chunks.p, (const pg::SegDesc*)ctx->s_seg.p, (const pg::Transition*)ctx->s_trans.p,
           off, (const pg::IntegralDesc*)ctx->s_desc.p, (const uint8_t*)ctx->s_act.p, (const double*)ctx->s_left.p,
           (const double*)ctx->s_len.p, n, (const int32_t*)ctx->s_bis.p, val, (double*)ctx->s_out_left.p,
-          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out, 0u, nullptr, 0, nullptr, 0);
+          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out, 0u, nullptr, 0, nullptr);
     else
       pg::compact_split_kernel<16><<<(unsigned)nch, pg::kRedThreads, 0, s>>>(
           (const pg::ChunkRef*)ctx->s_chunks.p, (const pg::SegDesc*)ctx->s_seg.p, (const pg::Transition*)ctx->s_trans.p,
           off, (const pg::IntegralDesc*)ctx->s_desc.p, (const uint8_t*)ctx->s_act.p, (const double*)ctx->s_left.p,
           (const double*)ctx->s_len.p, n, (const int32_t*)ctx->s_bis.p, val, (double*)ctx->s_out_left.p,
-          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out, 0u, nullptr, 0, nullptr, 0);
+          (double*)ctx->s_out_len.p, 2 * A, (uint32_t*)ctx->s_owner.p, par_out, 0u, nullptr, 0, nullptr);
     ctx->eng->stats.launches++;
   };
   launch((const double*)ctx->s_est.p, (double*)ctx->s_par.p);

@@ -148,13 +148,13 @@ Engine::~Engine() {
   cudaSetDevice(device);
   DevBuf* dev_bufs[] = {&rule_trie_, &rule_leafset_, &rule_code_, &rule_w_, &rule_scale_, &rule_norm_, &left_[0], &left_[1], &len_[0], &len_[1],
                         &owner_[0], &owner_[1], &parent_[0], &parent_[1], &est_, &err_a_, &err_b_, &bisect_,
-                        &terms_, &cache_,
+                        &terms_[0], &terms_[1], &ppos_[0], &ppos_[1], &chk_,
                         &active_, &partials_, &chunk_off_, &chunks_, &segs_, &trans_, &descs_, &scal_, &live_,
-                        &thr_out_, &thr_counts_, &adm_starts_, &adm_ids_, &rst_items_};
+                        &thr_out_, &thr_counts_, &adm_starts_, &adm_ids_, &rst_items_, &chain_, &chain_ts_};
   for (DevBuf* b : dev_bufs)
     if (b->p) cudaFree(b->p);
   DevBuf* host_bufs[] = {&h_segs_, &h_chunks_, &h_trans_, &h_trans_spill_, &h_scal_, &h_live_, &h_thr_,
-                         &h_adm_starts_, &h_adm_ids_, &h_rst_items_, &h_thr_counts_};
+                         &h_adm_starts_, &h_adm_ids_, &h_rst_items_, &h_thr_counts_, &h_chain_, &h_chk_};
   for (DevBuf* b : host_bufs)
     if (b->p) cudaFreeHost(b->p);
   for (auto& e : ev_)
@@ -346,7 +346,9 @@ int Engine::init(std::string* why) {
   rule_ = R;
   if ((rc = ensure(thr_out_, 64)) != PG_OK || (rc = ensure_pinned(h_thr_, 64)) != PG_OK ||
       (rc = ensure(thr_counts_, kMaxThresholds * 8)) != PG_OK ||
-      (rc = ensure_pinned(h_thr_counts_, kMaxThresholds * 8)) != PG_OK) {
+      (rc = ensure_pinned(h_thr_counts_, kMaxThresholds * 8)) != PG_OK || (rc = ensure(chain_, 64 * 8)) != PG_OK ||
+      (rc = ensure_pinned(h_chain_, 64 * 8)) != PG_OK || (rc = ensure(chain_ts_, sizeof(ThresholdSet))) != PG_OK ||
+      (rc = ensure(chk_, 64)) != PG_OK || (rc = ensure_pinned(h_chk_, 64)) != PG_OK) {
     if (why) *why = last_error;
     return rc;
   }
@@ -390,13 +392,15 @@ int Engine::evaluate(const IntegralDesc& desc, uint64_t n, const double* d_left,
 
 // One pass of the threshold kernels over integral jidx's chunks; out = {sum
 // err*flag, sum est*flag, count, min err, max err}.
-int Engine::threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5]) {
+// Without readback the pass is only enqueued (its flags and chunk offsets feed
+// the compaction later on the stream).
+int Engine::threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5],
+                           bool readback) {
   const SegDesc& S = ((const SegDesc*)h_segs_.p)[jidx];
   if (S.nchunks) {
-    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>((const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p,
-                                                             S.chunk_start, (const double*)est_.p,
-                                                             (const double*)err_b_.p, thr, write_flags, minmax,
-                                                             (uint8_t*)active_.p, (Partial*)partials_.p);
+    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(
+        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, S.chunk_start, (const double*)est_.p,
+        (const double*)err_b_.p, thr, nullptr, write_flags, minmax, (uint8_t*)active_.p, (Partial*)partials_.p);
     stats.launches++;
   }
   threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>((const SegDesc*)segs_.p, jidx,
@@ -404,6 +408,7 @@ int Engine::threshold_pass(uint32_t jidx, double thr, int write_flags, int minma
                                                             scan, (double*)thr_out_.p);
   stats.launches++;
   PG_TRY(cudaGetLastError(), "threshold launch");
+  if (!readback) return PG_OK;
   PG_TRY(cudaMemcpyAsync(h_thr_.p, thr_out_.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
          "threshold readback");
   PG_TRY(cudaStreamSynchronize(stream_), "threshold pass");
@@ -429,7 +434,7 @@ int Engine::threshold_counts(uint32_t jidx, const double* thr, int k, uint64_t* 
   PG_TRY(cudaMemsetAsync(thr_counts_.p, 0, kMaxThresholds * 8, stream_), "threshold counts");
   if (S.nchunks) {
     threshold_count_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(
-        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, S.chunk_start, (const double*)err_b_.p, ts,
+        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, S.chunk_start, (const double*)err_b_.p, ts, nullptr,
         (unsigned long long*)thr_counts_.p);
     stats.launches++;
   }
@@ -439,6 +444,54 @@ int Engine::threshold_counts(uint32_t jidx, const double* thr, int k, uint64_t* 
   stats.classify_passes++;
   std::memcpy(counts, h_thr_counts_.p, k * 8);
   stats.d2h_bytes += k * 8;
+  return PG_OK;
+}
+
+// The classifier's first three passes with one host round trip: the min/max
+// pass, the counts above the 20 thresholds of the raise sequence (built on
+// the device from the maximum), and the pass at the threshold where the raise
+// loop stops (chosen on the device from the counts).  The host repeats the
+// sequence and the choice with the same operations and takes the results from
+// h_chain_.
+int Engine::classify_chain(uint32_t jidx, double thr0, double pct, uint64_t n) {
+  const SegDesc& S = ((const SegDesc*)h_segs_.p)[jidx];
+  double* cb = (double*)chain_.p;
+  unsigned long long* cnt = (unsigned long long*)(cb + 16);
+  ThresholdSet* ts = (ThresholdSet*)chain_ts_.p;
+  const ChunkRef* ch = (const ChunkRef*)chunks_.p;
+  const SegDesc* sg = (const SegDesc*)segs_.p;
+  ThresholdSet none;
+  std::memset(&none, 0, sizeof none);
+  if (S.nchunks) {
+    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)est_.p,
+                                                             (const double*)err_b_.p, INFINITY, nullptr, 0, 1,
+                                                             (uint8_t*)active_.p, (Partial*)partials_.p);
+    stats.launches++;
+  }
+  threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>(sg, jidx, (const Partial*)partials_.p,
+                                                            (uint64_t*)chunk_off_.p, 0, cb);
+  threshold_seq_kernel<<<1, 32, 0, stream_>>>(cb, thr0, ts, cb + 40);
+  PG_TRY(cudaMemsetAsync(cnt, 0, kMaxThresholds * 8, stream_), "threshold counts");
+  if (S.nchunks) {
+    threshold_count_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)err_b_.p,
+                                                                   none, ts, cnt);
+    stats.launches++;
+  }
+  threshold_select_kernel<<<1, 32, 0, stream_>>>(cnt, cb + 40, n, pct, cb + 60);
+  if (S.nchunks) {
+    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)est_.p,
+                                                             (const double*)err_b_.p, 0.0, cb + 60, 0, 0,
+                                                             (uint8_t*)active_.p, (Partial*)partials_.p);
+    stats.launches++;
+  }
+  threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>(sg, jidx, (const Partial*)partials_.p,
+                                                            (uint64_t*)chunk_off_.p, 0, cb + 8);
+  stats.launches += 4;
+  PG_TRY(cudaGetLastError(), "threshold chain launch");
+  PG_TRY(cudaMemcpyAsync(h_chain_.p, cb, 64 * 8, cudaMemcpyDeviceToHost, stream_), "threshold chain readback");
+  PG_TRY(cudaStreamSynchronize(stream_), "threshold chain");
+  stats.classify_passes++;
+  stats.d2h_bytes += 64 * 8;
   return PG_OK;
 }
 
@@ -452,24 +505,37 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
   double o[5];
   int rc;
   const auto t_cls = std::chrono::steady_clock::now();
-  if ((rc = threshold_pass(jidx, INFINITY, 0, 1, 0, o)) != PG_OK) return rc;
+  const double thr0 = iter_err / (double)n;
+  // A first raise step is certain (nothing passes before it); with a
+  // non-negative start its three passes run chained, with one round trip.
+  bool first = thr0 >= 0.0;
+  const double* hc = (const double*)h_chain_.p;
+  if (first) {
+    if ((rc = classify_chain(jidx, thr0, C.max_active_regions_percentage, n)) != PG_OK) return rc;
+    std::memcpy(o, hc, sizeof o);
+  } else if ((rc = threshold_pass(jidx, INFINITY, 0, 1, 0, o)) != PG_OK) {
+    return rc;
+  }
   const double mn = o[3], mx = o[4];
-  double low = mn, high = mx, thr = iter_err / (double)n, flags_thr = thr;
+  double low = mn, high = mx, thr = thr0, flags_thr = thr;
   bool pass_mem = false, pass_budget = false;
   uint64_t num_active = 0;
   double dot_err = 0, dot_est = 0, finished_errorest = 0;
   const double target = std::fabs(C.last[2]) * C.epsrel;
   uint64_t inc = 0, dec = 0;
-  auto apply = [&](double t) -> int {
-    double q[5];
-    int r2 = threshold_pass(jidx, t, 0, 0, 0, q);
-    if (r2 != PG_OK) return r2;
+  auto take = [&](const double* q, double t) {
     flags_thr = t;
     dot_err = q[0];
     dot_est = q[1];
     num_active = (uint64_t)q[2];
     const double pct = (double)(int)num_active / (double)(int)n;
     pass_mem = pct <= C.max_active_regions_percentage;
+  };
+  auto apply = [&](double t) -> int {
+    double q[5];
+    int r2 = threshold_pass(jidx, t, 0, 0, 0, q);
+    if (r2 != PG_OK) return r2;
+    take(q, t);
     return PG_OK;
   };
   do {
@@ -496,12 +562,21 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
         t += std::fabs(high - t) * .5;
       }
       uint64_t cnt[kMaxThresholds];
-      if ((rc = threshold_counts(jidx, seq, kMaxThresholds, cnt)) != PG_OK) return rc;
+      // the chain's sequence is this one, bit for bit (same operations)
+      const bool chained = first && std::memcmp(seq, hc + 40, sizeof seq) == 0;
+      first = false;
+      if (chained)
+        std::memcpy(cnt, hc + 16, sizeof cnt);
+      else if ((rc = threshold_counts(jidx, seq, kMaxThresholds, cnt)) != PG_OK)
+        return rc;
       int stop = -1;
       for (int q = 0; q < kMaxThresholds && stop < 0; ++q)
         if ((double)(int)cnt[q] / (double)(int)n <= C.max_active_regions_percentage) stop = q;
       const int last = stop >= 0 ? stop : kMaxThresholds - 1;
-      if ((rc = apply(seq[last])) != PG_OK) return rc;
+      if (chained && std::memcmp(&seq[last], hc + 60, 8) == 0)
+        take(hc + 8, seq[last]);
+      else if ((rc = apply(seq[last])) != PG_OK)
+        return rc;
       if (stop >= 0) {
         if (stop > 0) low = seq[stop - 1];
         thr = seq[stop];
@@ -543,7 +618,7 @@ int Engine::classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err,
   *ok_out = ok;
   *num_active_out = num_active;
   if (ok) {
-    if ((rc = threshold_pass(jidx, flags_thr, 1, 0, 1, o)) != PG_OK) return rc;
+    if ((rc = threshold_pass(jidx, flags_thr, 1, 0, 1, o, false)) != PG_OK) return rc;  // flags for the compaction
     *fin_est_out = iter_est - dot_est;
     *fin_err_out = finished_errorest;
   }
@@ -607,9 +682,22 @@ int Engine::grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_
   return PG_OK;
 }
 
+// The bounds record of the term lookups, read after a synchronisation: a
+// recorded check means a lookup was skipped and the run's results are void.
+int Engine::check_bounds() {
+  const unsigned long long* r = (const unsigned long long*)h_chk_.p;
+  if (r[0] == 0) return PG_OK;
+  static const char* what[] = {"", "parent index", "parent position", "term position", "parent record"};
+  last_error = std::string("set-sum term lookup out of bounds: ") + what[r[0] < 5 ? r[0] : 0] + " " +
+               std::to_string(r[1]) + " >= " + std::to_string(r[2]) + " (integral " + std::to_string(r[3]) +
+               ", segment start " + std::to_string(r[4]) + ", regions " + std::to_string(r[5]) + ", position " +
+               std::to_string(r[6]) + ")";
+  return PG_CUDA_ERROR;
+}
+
 int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
-                    uint64_t out_stride, uint32_t* out_owner, double* parent_out, const double* terms,
-                    int terms_rows, double* cache_out, int cache_rows) {
+                    uint64_t out_stride, uint32_t* out_owner, double* parent_out, uint32_t* ppos_out,
+                    uint64_t ppos_n) {
   (void)nxt;
   if (nchunks == 0) return PG_OK;
   if (maxd <= 8) {
@@ -617,15 +705,15 @@ int Engine::compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int max
         (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
         (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
         (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
-        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0, terms, terms_rows,
-        cache_out, cache_rows);
+        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0, ppos_out, ppos_n,
+        (unsigned long long*)chk_.p);
   } else {
     compact_split_kernel<16><<<nchunks, kRedThreads, 0, stream_>>>(
         (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, (const Transition*)trans_.p,
         (const uint64_t*)chunk_off_.p, (const IntegralDesc*)descs_.p, (const uint8_t*)active_.p,
         (const double*)left_[cur].p, (const double*)len_[cur].p, reg_cap_[cur], (const int32_t*)bisect_.p,
-        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0, terms, terms_rows,
-        cache_out, cache_rows);
+        (const double*)est_.p, out_left, out_len, out_stride, out_owner, parent_out, chunk0, ppos_out, ppos_n,
+        (unsigned long long*)chk_.p);
   }
   stats.launches++;
   PG_TRY(cudaGetLastError(), "compact/split launch");
@@ -675,10 +763,14 @@ int Engine::evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& l
     L.base = R.start;
     L.scale = R.scale;
     if (R.mode == PG_EVAL_SET_SUMS && terms_rows_ > 0) {
-      L.pcache = cache_.p ? (const double*)cache_.p : nullptr;
-      L.pcache_rows = terms_rows_ + 1;
-      L.terms = (double*)terms_.p;
+      L.pterms = (const double*)terms_[cur ^ 1].p;
+      L.ppos = (const uint32_t*)ppos_[cur].p;
+      L.terms = (double*)terms_[cur].p;
       L.terms_rows = terms_rows_;
+      L.terms_n = terms_n_[cur];
+      L.pterms_n = terms_n_[cur ^ 1];
+      L.ppos_n = ppos_n_[cur];
+      L.chk = (unsigned long long*)chk_.p;
     }
     PG_TRY(launch(L), "evaluation launch");
     stats.launches++;
@@ -704,11 +796,11 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     const char* env = std::getenv("PG_SETSUM_CACHE");
     if (env && env[0] == '0') use_cache = false;
   }
-  const int term_rows = kTermValues * maxd;  // + one row for the split axis in the parents' cache
+  const int term_rows = kTermValues * maxd + 1;  // the per-axis terms and the split axis
   // Pool capacity in regions: both region lists, owners, parents and the
-  // per-region scratch of one iteration (with the kept terms: this list's and
-  // its parents', half as many).
-  const uint64_t bytes_per_region = 32ull * maxd + 53 + (use_cache ? 8ull * term_rows + 4ull * (term_rows + 1) : 0);
+  // per-region scratch of one iteration (with the kept terms: both lists'
+  // terms and parent positions).
+  const uint64_t bytes_per_region = 32ull * maxd + 53 + (use_cache ? 16ull * term_rows + 4 : 0);
   uint64_t cap = policy.max_regions;
   if (cap == 0) {
     size_t fr = 0, tot = 0;
@@ -717,6 +809,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
   }
   if (policy.budget_bytes) cap = std::min<uint64_t>(cap, policy.budget_bytes / bytes_per_region);
   cap = std::max<uint64_t>(cap, 4096);
+  if (cap >= (1ull << 32)) use_cache = false;  // parent positions are 32-bit
   const uint64_t admit_limit = (uint64_t)(policy.admit_fraction * (double)cap);
   // Per-integral arrays.
   if ((rc = ensure(descs_, njobs * sizeof(IntegralDesc))) != PG_OK) return rc;
@@ -763,6 +856,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     J.sp_off = J.sp_poff = 0;
   }
   spill_.reset();
+  PG_TRY(cudaMemsetAsync(chk_.p, 0, 64, stream_), "bounds record");
+  terms_n_[0] = terms_n_[1] = ppos_n_[0] = ppos_n_[1] = 0;
   spill_batches_.clear();
   const auto t_start = std::chrono::steady_clock::now();
   // Host decision time: from the end of an iteration's readback to the next
@@ -968,7 +1063,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     if ((rc = ensure(bisect_, N * 4)) != PG_OK) return rc;
     if ((rc = ensure(active_, N)) != PG_OK) return rc;
     terms_rows_ = use_cache ? term_rows : 0;
-    if (use_cache && (rc = ensure(terms_, div_up(N, 32) * 256 * (uint64_t)term_rows)) != PG_OK) return rc;
+    if (use_cache && (rc = ensure(terms_[cur], div_up(N, 32) * 256 * (uint64_t)term_rows)) != PG_OK) return rc;
+    terms_n_[cur] = use_cache ? N : 0;
     if ((rc = ensure(partials_, nchunks * sizeof(Partial))) != PG_OK) return rc;
     if ((rc = ensure(chunk_off_, nchunks * 8)) != PG_OK) return rc;
     if ((rc = ensure(chunks_, nchunks * sizeof(ChunkRef))) != PG_OK) return rc;
@@ -996,8 +1092,8 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       stats.points_evaluated += J.n * (uint64_t)rule_.feval[J.desc.d];
       stats.eval_bytes += J.n * (16ull * d + 24ull);  // + the 4-byte owner of a shared list
       if (use_cache && job_eval_mode(J) == PG_EVAL_SET_SUMS) {
-        stats.eval_bytes += J.n * 8ull * kTermValues * d;  // the terms written
-        if (J.has_cache) stats.eval_bytes += (J.n / 2) * (8ull * kTermValues * (d - 1) + 8ull);  // parents' read
+        stats.eval_bytes += J.n * (8ull * kTermValues * d + 8);  // the terms and split axes written
+        if (J.has_cache) stats.eval_bytes += (J.n / 2) * (8ull * kTermValues * (d - 1) + 12ull);  // parents' read
       }
     }
     if (profiling) cudaEventRecord(ev_[1], stream_);
@@ -1015,7 +1111,9 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
            "scalar readback");
     {
       const auto w0 = std::chrono::steady_clock::now();
+      PG_TRY(cudaMemcpyAsync(h_chk_.p, chk_.p, 64, cudaMemcpyDeviceToHost, stream_), "bounds record");
       PG_TRY(cudaStreamSynchronize(stream_), "iteration");
+      if ((rc = check_bounds()) != PG_OK) return rc;
       t_decision = std::chrono::steady_clock::now();
       decision_open = true;
       stats.sync_ms += std::chrono::duration<double, std::milli>(t_decision - w0).count();
@@ -1252,13 +1350,12 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       if ((rc = grow_list(nxt, out_total, maxd, 0, 0)) != PG_OK) return rc;
       // This iteration's evaluation has read the parents' terms; the cache now
       // takes the terms of the regions being bisected.
-      if (use_cache && (rc = ensure(cache_, div_up(par_total, 32) * 256 * (uint64_t)(term_rows + 1))) != PG_OK)
-        return rc;
+      if (use_cache && (rc = ensure(ppos_[nxt], par_total * 4)) != PG_OK) return rc;
+      ppos_n_[nxt] = use_cache ? par_total : 0;
       if (profiling) cudaEventRecord(ev_[4], stream_);
       if ((rc = compact(cur, nxt, 0, (uint32_t)nchunks, maxd, (double*)left_[nxt].p, (double*)len_[nxt].p,
                         reg_cap_[nxt], (uint32_t*)owner_[nxt].p, (double*)parent_[nxt].p,
-                        use_cache ? (const double*)terms_.p : nullptr, term_rows,
-                        use_cache ? (double*)cache_.p : nullptr, term_rows + 1)) != PG_OK)
+                        use_cache ? (uint32_t*)ppos_[nxt].p : nullptr, ppos_n_[nxt])) != PG_OK)
         return rc;
       if (profiling) {
         cudaEventRecord(ev_[5], stream_);
@@ -1271,7 +1368,7 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
       if (J.state != JOB_RESIDENT || Tr.mode == 0) continue;
       stats.stage_bytes += J.n + Tr.A * (uint64_t)(16 * J.desc.d + 12) + 2 * Tr.A * (uint64_t)(16 * J.desc.d + 4) +
                            Tr.A * 8;
-      if (Tr.cache) stats.stage_bytes += Tr.A * (uint64_t)(16 * kTermValues * J.desc.d + 8);  // terms kept
+      if (Tr.cache) stats.stage_bytes += Tr.A * 4;  // the parents' positions
       J.start = Tr.out_start;
       J.n = 2 * Tr.A;
       J.par_start = Tr.par_out;
@@ -1282,7 +1379,9 @@ int Engine::run(std::vector<Job>& jobs, const EvalLauncher& launch, const RunPol
     P = par_total;
     cur = nxt;
   }
+  PG_TRY(cudaMemcpyAsync(h_chk_.p, chk_.p, 64, cudaMemcpyDeviceToHost, stream_), "bounds record");
   PG_TRY(cudaStreamSynchronize(stream_), "run");
+  if ((rc = check_bounds()) != PG_OK) return rc;
   if (profiling && compact_timing_pending_) record(ev_[4], ev_[5], &stats.stage_ms);
   if (profiling && spill_timing_pending_) record(ev_[6], ev_[7], &stats.spill_ms);
   if (profiling && admit_timing_pending_) record(ev_[8], ev_[9], &stats.admit_ms);
@@ -1368,10 +1467,14 @@ cudaError_t launch_family_eval(const EvalLaunch& L) {
   const pg_eval_args a = eval_args_of(L);
   if (L.mode == PG_EVAL_SET_SUMS) {
     SetSumCache c;
-    c.pcache = L.pcache;
-    c.pcache_rows = L.pcache_rows;
+    c.pterms = L.pterms;
+    c.ppos = L.ppos;
     c.terms = L.terms;
     c.terms_rows = L.terms_rows;
+    c.terms_n = L.terms_n;
+    c.pterms_n = L.pterms_n;
+    c.ppos_n = L.ppos_n;
+    c.chk = L.chk;
     c.scale = L.scale;
     return launch_setsum(a, L.segs, L.base, c);
   }

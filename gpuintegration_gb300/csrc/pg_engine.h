@@ -46,10 +46,12 @@ struct EvalLaunch {
   uint64_t base = 0;
   // Set-sum kernel only: the parents' kept terms and this list's terms
   // (null: none kept / none written).
-  const double* pcache = nullptr;
-  int pcache_rows = 0;
+  const double* pterms = nullptr;
+  const uint32_t* ppos = nullptr;
   double* terms = nullptr;
   int terms_rows = 0;
+  uint64_t terms_n = 0, pterms_n = 0, ppos_n = 0;
+  unsigned long long* chk = nullptr;
   bool scale = true;  // some integral of the launch has a Jacobian other than 1
 };
 
@@ -120,7 +122,7 @@ struct Job {
   uint64_t start = 0;  // first region in the current list
   uint64_t par_start = 0;
   int has_parent = 0;
-  int has_cache = 0;  // its parents' per-axis terms are in the engine's parent cache
+  int has_cache = 0;  // its parents' per-axis terms are in the previous list's term buffer
   int iters = 0;
   bool done = false;
   int error = 0;
@@ -242,13 +244,16 @@ class Engine {
   int fail(cudaError_t e, const char* what);
   int classify_job(Job& J, uint32_t jidx, double iter_err, double fin_err, bool* ok, double* fin_est_out,
                    double* fin_err_out, uint64_t* num_active, double iter_est);
-  int threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5]);
+  int threshold_pass(uint32_t jidx, double thr, int write_flags, int minmax, int scan, double out[5],
+                     bool readback = true);
+  int classify_chain(uint32_t jidx, double thr0, double pct, uint64_t n);
   // Counts of integral jidx's errors above each of the k thresholds (one pass).
   int threshold_counts(uint32_t jidx, const double* thr, int k, uint64_t* counts);
   int grow_list(int which, uint64_t need, int rows, uint64_t live, uint64_t live_par);
   int compact(int cur, int nxt, uint32_t chunk0, uint32_t nchunks, int maxd, double* out_left, double* out_len,
-              uint64_t out_stride, uint32_t* out_owner, double* parent_out, const double* terms = nullptr,
-              int terms_rows = 0, double* cache_out = nullptr, int cache_rows = 0);
+              uint64_t out_stride, uint32_t* out_owner, double* parent_out, uint32_t* ppos_out = nullptr,
+              uint64_t ppos_n = 0);
+  int check_bounds();
   // Launches the evaluation of list `cur`'s regions [0, N): one launch per
   // maximal range of resident integrals that share an evaluation kernel.
   int evaluate_list(std::vector<Job>& jobs, const std::vector<uint32_t>& live, int cur, uint64_t N,
@@ -264,15 +269,21 @@ class Engine {
   int reg_rows_[2] = {0, 0};
   // per-region scratch
   DevBuf est_, err_a_, err_b_, bisect_, active_;
-  // set-sum evaluation: this list's per-axis terms (tiles of terms_rows_ rows
-  // by list position) and the kept parents' (tiles of terms_rows_ + 1 rows by
-  // parent index; the extra row holds the split axis)
-  DevBuf terms_, cache_;
+  // set-sum evaluation: each list's per-axis terms and split axes (tiles of
+  // terms_rows_ rows by list position), and per list the positions of its
+  // parents in the other list (by parent index)
+  DevBuf terms_[2], ppos_[2];
   int terms_rows_ = 0;
+  uint64_t terms_n_[2] = {0, 0}, ppos_n_[2] = {0, 0};  // positions with terms, parents with positions
+  DevBuf chk_, h_chk_;                                // bounds record of the term lookups
   // per-chunk
   DevBuf partials_, chunk_off_, chunks_;
   // per-integral
   DevBuf segs_, trans_, descs_, scal_, live_, thr_out_, thr_counts_, adm_starts_, adm_ids_;
+  // The classifier's chained first passes: [0..4] min/max pass, [8..12] pass
+  // at the chosen threshold, [16..35] counts (u64), [40..59] the threshold
+  // sequence, [60] the chosen threshold; and the device-built threshold set.
+  DevBuf chain_, h_chain_, chain_ts_;
   // restore table of one admission (device, and its pinned host mirror)
   DevBuf rst_items_, h_rst_items_;
   SpillArena spill_;

@@ -37,6 +37,25 @@ __host__ __device__ __forceinline__ uint64_t term_at(uint64_t pos, int row, int 
   return ((pos >> 5) * (uint64_t)rows + (uint64_t)row) * 32ull + (pos & 31ull);
 }
 
+// Bounds checks of the term lookups: the first index found outside its
+// buffer is recorded (rec[0] = check code, rec[1] = index, rec[2] = bound,
+// rec[3..6] = integral, segment start, regions, list position) and the access
+// is skipped; the host reads the record after each iteration and fails the
+// run.
+__device__ __forceinline__ bool in_bounds(unsigned long long* rec, int code, uint64_t i, uint64_t bound,
+                                          uint64_t a = 0, uint64_t b = 0, uint64_t c = 0, uint64_t e = 0) {
+  if (i < bound) return true;
+  if (rec && atomicCAS(rec, 0ull, (unsigned long long)code) == 0ull) {
+    rec[1] = i;
+    rec[2] = bound;
+    rec[3] = a;
+    rec[4] = b;
+    rec[5] = c;
+    rec[6] = e;
+  }
+  return false;
+}
+
 // Segment of one integral in the current region list.
 struct SegDesc {
   uint64_t start;      // first region
@@ -78,7 +97,7 @@ struct Transition {
   uint64_t A;          // kept regions (children: 2A)
   uint64_t par_out;    // first parent estimate written for the next iteration
   int32_t mode;        // 0 drop, 1 keep the flagged regions, 2 keep every region
-  int32_t cache;       // 1: keep the kept regions' per-axis terms for their children
+  int32_t cache;       // 1: record the kept regions' positions for their children's term lookups
 };
 
 // ---------------------------------------------------------------------------
@@ -241,8 +260,7 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
                          const int32_t* __restrict__ bisect, const double* __restrict__ est,
                          double* __restrict__ out_left, double* __restrict__ out_length, uint64_t out_stride,
                          uint32_t* __restrict__ out_owner, double* __restrict__ parent_out, uint32_t chunk0,
-                         const double* __restrict__ terms, int terms_rows, double* __restrict__ cache_out,
-                         int cache_rows) {
+                         uint32_t* __restrict__ ppos_out, uint64_t ppos_n, unsigned long long* __restrict__ chk) {
   __shared__ uint32_t wcount[kRedThreads / 32];
   const uint32_t cidx = chunk0 + blockIdx.x;
   const ChunkRef cr = chunks[cidx];
@@ -305,15 +323,9 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
         out_owner[c1] = cr.integral;
       }
       parent_out[T.par_out + pos] = e;
-      if (cache_out && T.cache) {
-        // The region's per-axis terms for its children, and the axis it is
-        // split on (the one axis whose terms the children evaluate).
-        const int rows = kTermValues * d;
-        const uint64_t pj = T.par_out + pos;
-#pragma unroll 4
-        for (int q = 0; q < rows; ++q) cache_out[term_at(pj, q, cache_rows)] = terms[term_at(i, q, terms_rows)];
-        cache_out[term_at(pj, rows, cache_rows)] = (double)bd;
-      }
+      // where the children find the region's per-axis terms: its position
+      // in this list's term buffer
+      if (ppos_out && T.cache && in_bounds(chk, 4, T.par_out + pos, ppos_n)) ppos_out[T.par_out + pos] = (uint32_t)i;
     }
     run += total;
     __syncthreads();  // wcount is rewritten by the next slice
@@ -328,8 +340,10 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
 // ---------------------------------------------------------------------------
 static __global__ void __launch_bounds__(kRedThreads)
     threshold_kernel(const ChunkRef* __restrict__ chunks, const SegDesc* __restrict__ segs, uint32_t chunk0,
-                     const double* __restrict__ est, const double* __restrict__ err, double thr, int write_flags,
-                     int minmax, uint8_t* __restrict__ active, Partial* __restrict__ partials) {
+                     const double* __restrict__ est, const double* __restrict__ err, double thr_arg,
+                     const double* __restrict__ thr_dev, int write_flags, int minmax, uint8_t* __restrict__ active,
+                     Partial* __restrict__ partials) {
+  const double thr = thr_dev ? *thr_dev : thr_arg;  // a threshold chosen on the device, else the argument
   __shared__ NS scratch[8];
   __shared__ unsigned long long cnt_s;
   __shared__ double mm[2][8];
@@ -399,10 +413,17 @@ struct ThresholdSet {
 
 static __global__ void __launch_bounds__(kRedThreads)
     threshold_count_kernel(const ChunkRef* __restrict__ chunks, const SegDesc* __restrict__ segs, uint32_t chunk0,
-                           const double* __restrict__ err, ThresholdSet ts, unsigned long long* __restrict__ counts) {
+                           const double* __restrict__ err, ThresholdSet ts_arg, const ThresholdSet* __restrict__ ts_dev,
+                           unsigned long long* __restrict__ counts) {
   __shared__ unsigned long long sc[kMaxThresholds];
-  if (threadIdx.x < kMaxThresholds) sc[threadIdx.x] = 0ull;
+  __shared__ ThresholdSet ts_s;  // the set built on the device, else the argument
+  if (threadIdx.x < kMaxThresholds) {
+    sc[threadIdx.x] = 0ull;
+    ts_s.bits[threadIdx.x] = ts_dev ? ts_dev->bits[threadIdx.x] : ts_arg.bits[threadIdx.x];
+  }
+  if (threadIdx.x == 0) ts_s.k = ts_dev ? ts_dev->k : ts_arg.k;
   __syncthreads();
+  const ThresholdSet& ts = ts_s;
   const ChunkRef cr = chunks[chunk0 + blockIdx.x];
   const SegDesc S = segs[cr.integral];
   uint32_t c[kMaxThresholds];
@@ -426,6 +447,38 @@ static __global__ void __launch_bounds__(kRedThreads)
   }
   __syncthreads();
   if (threadIdx.x < ts.k && sc[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
+}
+
+// The classifier's raise sequence t_0 = thr0, t_(q+1) = t_q + |max - t_q| / 2
+// (heuristic_classifier.cuh:380-395), max being the largest error of a
+// min/max pass (mm[4]), built on the device so the counting pass can follow
+// the min/max pass without a host round trip.  The host forms the same
+// sequence with the same operations.
+static __global__ void threshold_seq_kernel(const double* __restrict__ mm, double thr0, ThresholdSet* __restrict__ ts,
+                                            double* __restrict__ seq) {
+  if (threadIdx.x != 0) return;
+  const double high = mm[4];
+  double t = thr0;
+  for (int q = 0; q < kMaxThresholds; ++q) {
+    seq[q] = t;
+    ts->bits[q] = (unsigned long long)__double_as_longlong(__dadd_rn(t, 0.0));  // +0 for a -0 threshold
+    t = __dadd_rn(t, __dmul_rn(fabs(__dsub_rn(high, t)), 0.5));
+  }
+  ts->k = kMaxThresholds;
+}
+
+// Where the raise loop stops: the first threshold of the sequence that leaves
+// at most the share `pct` of the n regions active, else the last
+// (heuristic_classifier.cuh:380-395, with the reference's int conversions);
+// its value goes to *sel for the pass at that threshold.
+static __global__ void threshold_select_kernel(const unsigned long long* __restrict__ counts,
+                                               const double* __restrict__ seq, uint64_t n, double pct,
+                                               double* __restrict__ sel) {
+  if (threadIdx.x != 0) return;
+  int stop = -1;
+  for (int q = 0; q < kMaxThresholds && stop < 0; ++q)
+    if (__ddiv_rn((double)(int)counts[q], (double)(int)n) <= pct) stop = q;
+  *sel = seq[stop >= 0 ? stop : kMaxThresholds - 1];
 }
 
 // Merge of threshold partials of one integral (same order as finalize_kernel)

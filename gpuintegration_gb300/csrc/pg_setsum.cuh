@@ -46,13 +46,14 @@
 // eval_kernel.
 //
 // Parent terms: a region's eight values per axis (c, h(+G0), h(-G0),
-// h(+G1), h(-G1), p2, p3, p4; p0 and p1 are sums of the second to fifth) are
-// written to `terms`, and the compaction keeps those of the regions it
-// bisects, with the split axis in one more row.  Both children of a region
-// share its coordinates on every axis but the split one, so a pair whose
-// parent's values are kept takes them from there and evaluates only the split
-// axis's factors: 22 per pair instead of 99 at d = 8.  The values are those
-// the children would compute, bit for bit.
+// h(+G1), h(-G1), p2, p3, p4; p0 and p1 are sums of the second to fifth) and
+// its split axis (one more row) are written to `terms`, the list's term
+// buffer, and stay there while the next list is evaluated; the compaction
+// records each bisected region's position in that buffer (`ppos`, by parent
+// index).  Both children of a region share its coordinates on every axis but
+// the split one, so a pair whose parent's values are kept takes them from
+// there and evaluates only the split axis's factors: 22 per pair instead of
+// 99 at d = 8.  The values are those the children would compute, bit for bit.
 //
 // One thread per region or sibling pair: with a thread per region every FP64
 // warp instruction carries 32 regions' work, and the SoA loads of the bounds
@@ -143,11 +144,11 @@ __device__ __forceinline__ void put_terms(double* __restrict__ terms, int rows, 
   t[7 * 32] = A.p4;
 }
 
-// One axis's terms of a parent, kept at parent index pidx; the five values the
-// fourth differences read go to fd[v * T].
-__device__ __forceinline__ AxisTerm cached_term(const double* __restrict__ cache, int rows, uint64_t pidx, int k,
+// One axis's terms of a parent at position ppos of the previous list's term
+// buffer; the five values the fourth differences read go to fd[v * T].
+__device__ __forceinline__ AxisTerm cached_term(const double* __restrict__ pterms, int rows, uint64_t ppos, int k,
                                                 double* fd, int T) {
-  const double* t = cache + term_at(pidx, k * kTermValues, rows);
+  const double* t = pterms + term_at(ppos, k * kTermValues, rows);
   double v[kTermValues];
 #pragma unroll
   for (int q = 0; q < kTermValues; ++q) v[q] = t[q * 32];
@@ -160,9 +161,9 @@ __device__ __forceinline__ AxisTerm cached_term(const double* __restrict__ cache
 // Factor value v of axis k is fv[(k * 5 + v) * T], except on axis `sk`, whose
 // values are at own[v * T].
 template <int MAXD, bool SCALE>
-__device__ __forceinline__ void region_result(const SetSumSmem<MAXD>& Sm, const RuleDev& rule, const SetSums& Q,
-                                              int d, double jac, double vol, int maxdim, const double* fv, int sk,
-                                              const double* own, double* est, double* err, int32_t* bisect) {
+__device__ __forceinline__ int region_result(const SetSumSmem<MAXD>& Sm, const RuleDev& rule, const SetSums& Q,
+                                             int d, double jac, double vol, int maxdim, const double* fv, int sk,
+                                             const double* own, double* est, double* err, int32_t* bisect) {
   constexpr int T = kSetSumThreads;
   // Jacobian scaling (a box other than the unit cube): compiled out of
   // launches whose integrals all have jac = 1, where a predicated multiply
@@ -255,7 +256,9 @@ __device__ __forceinline__ void region_result(const SetSumSmem<MAXD>& Sm, const 
   const bool ladder = PG_SETSUM_MUL(5.0, e1) <= e2 && PG_SETSUM_MUL(5.0, e2) <= e3;
   *est = PG_SETSUM_MUL(vol, s5[0]);
   *err = PG_SETSUM_MUL(vol, ladder ? e1 : PG_SETSUM_MUL(5.0, emax));
-  *bisect = cand >= 0 ? cand : maxdim;
+  const int axis = cand >= 0 ? cand : maxdim;
+  *bisect = axis;
+  return axis;
 }
 
 // Widest axis (first strictly widest; a negative or NaN side never wins) and
@@ -272,9 +275,10 @@ __device__ __forceinline__ void side_step(int k, double side, double& vol, unsig
 
 // Regions [0, n) of a run that starts at list position `base`, one per
 // thread, blocks in list order.  With `terms` (tiles of `terms_rows` rows,
-// by list position) every region's terms are written; with `pcache` (tiles of
-// `pcache_rows` rows, by parent index) pairs of segments flagged has_cache
-// take their shared axes' terms from their parent.
+// by list position) every region's terms are written; with `pterms` (the
+// previous list's term buffer, same rows) and `ppos` (parent index -> its
+// position there), pairs of segments flagged has_cache take their shared
+// axes' terms from their parent.
 // (A grid-stride loop over tens of millions of regions lets the blocks drift
 // apart over the list, and the scattered loads
 // of the SoA rows made each region up to 40% dearer.)  With `segs` (the
@@ -287,8 +291,9 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
     setsum_kernel(const double* __restrict__ left, const double* __restrict__ length, uint64_t n, uint64_t stride,
                   const uint32_t* __restrict__ owner, const IntegralDesc* __restrict__ descs, RuleDev rule,
                   double* __restrict__ est, double* __restrict__ err, int32_t* __restrict__ bisect,
-                  const SegDesc* __restrict__ segs, uint64_t base, const double* __restrict__ pcache,
-                  int pcache_rows, double* __restrict__ terms, int terms_rows) {
+                  const SegDesc* __restrict__ segs, uint64_t base, const double* __restrict__ pterms,
+                  const uint32_t* __restrict__ ppos, double* __restrict__ terms, int terms_rows, uint64_t terms_n,
+                  uint64_t pterms_n, uint64_t ppos_n, unsigned long long* __restrict__ chk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SetSumSmem<MAXD>& Sm = *reinterpret_cast<SetSumSmem<MAXD>*>(smem_raw);
   constexpr int T = kSetSumThreads;
@@ -297,18 +302,25 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
   uint32_t j = 0;
   uint64_t rb = r;  // the sibling evaluated with r (r itself: none)
   bool cached = false;
-  uint64_t pidx = 0;  // the pair's parent index
+  uint64_t pp = 0;  // the pair's parent's position in the previous list
   if (work) {
     j = owner ? owner[r] : 0u;
     if (segs) {
       const SegDesc& S = segs[j];
       const uint64_t local = base + r - S.start, half = S.n / 2;
       if (S.has_parent && (S.n & 1ull) == 0ull && half > 0) {
-        if (local >= half) work = false;  // evaluated with its sibling
-        rb = r + half;
-        if (rb >= n) rb = r;  // a segment always lies inside one run; never read outside it
-        cached = pcache && S.has_cache && rb != r;
-        pidx = S.par_start + local;
+        if (local >= half) {
+          work = false;  // evaluated with its sibling; its parent index would be past the segment's parents
+        } else {
+          rb = r + half;
+          if (rb >= n) rb = r;  // a segment always lies inside one run; never read outside it
+          cached = pterms && S.has_cache && rb != r &&
+                   in_bounds(chk, 1, S.par_start + local, ppos_n, j, S.start, S.n, base + r);
+          if (cached) {
+            pp = ppos[S.par_start + local];
+            cached = in_bounds(chk, 2, pp, pterms_n, j, S.start, S.n, base + r);
+          }
+        }
       }
     }
   }
@@ -323,6 +335,7 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
   double* const fvb = Sm.fd + (MAXD * kFdValues) * T + threadIdx.x;
   if (!work) return;
   const bool pair = rb != r;
+  if (terms && !(in_bounds(chk, 3, base + r, terms_n) && in_bounds(chk, 3, base + rb, terms_n))) terms = nullptr;
   const IntegralDesc& D = descs[j];
   const int d = D.d;
   const bool unit = D.unit != 0;
@@ -332,7 +345,7 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
   // rounding, still differ from the parent on the split axis.)
   int s = d - 1;
   if (cached)
-    s = min(max((int)pcache[term_at(pidx, kTermValues * d, pcache_rows)], 0), d - 1);
+    s = min(max((int)pterms[term_at(pp, kTermValues * d, terms_rows)], 0), d - 1);
   else if (pair)
     for (int k = d - 1; k >= 0; --k)
       if (left[(uint64_t)k * stride + r] != left[(uint64_t)k * stride + rb]) s = k;
@@ -370,7 +383,7 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
     double* const fk = fv + (k * kFdValues) * T;
     AxisTerm A;
     if (cached)
-      A = (k == s) ? Ac : cached_term(pcache, pcache_rows, pidx, k, fk, T);
+      A = (k == s) ? Ac : cached_term(pterms, terms_rows, pp, k, fk, T);
     else
       A = axis_term(D, rule, k, lo, up, unit, fk, T);
     if (terms) {
@@ -387,12 +400,16 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
   {
     SetSums R = Q;
     set_step(R, As);
-    region_result<MAXD, SCALE>(Sm, rule, R, d, jac, vol, maxdim, fv, -1, fv, &est[r], &err[r], &bisect[r]);
+    const int ax = region_result<MAXD, SCALE>(Sm, rule, R, d, jac, vol, maxdim, fv, -1, fv, &est[r], &err[r],
+                                              &bisect[r]);
+    if (terms) terms[term_at(base + r, kTermValues * d, terms_rows)] = (double)ax;
   }
   if (pair) {
     SetSums R = Q;
     set_step(R, Bs);
-    region_result<MAXD, SCALE>(Sm, rule, R, d, jac, volb, maxdimb, fv, s, fvb, &est[rb], &err[rb], &bisect[rb]);
+    const int ax = region_result<MAXD, SCALE>(Sm, rule, R, d, jac, volb, maxdimb, fv, s, fvb, &est[rb], &err[rb],
+                                              &bisect[rb]);
+    if (terms) terms[term_at(base + rb, kTermValues * d, terms_rows)] = (double)ax;
   }
 }
 
@@ -400,10 +417,12 @@ static __global__ void __launch_bounds__(kSetSumThreads, PG_SETSUM_MIN_BLOCKS)
 // all have product-form families: one thread per region.  `segs` may be null
 // (no sibling pairing); `base` is the run's first list position.
 struct SetSumCache {
-  const double* pcache = nullptr;  // parents' terms, row k * 8 + v of tiles by parent index
-  int pcache_rows = 0;             // rows per tile (8 * the list's largest dimension + 1)
-  double* terms = nullptr;         // this list's terms, row k * 8 + v of tiles by list position
-  int terms_rows = 0;              // rows per tile (8 * the list's largest dimension)
+  const double* pterms = nullptr;  // the previous list's terms (the parents')
+  const uint32_t* ppos = nullptr;  // parent index -> the parent's position in the previous list
+  double* terms = nullptr;         // this list's terms: row k * 8 + v, then the split axis, tiles by position
+  int terms_rows = 0;              // rows per tile (8 * the list's largest dimension + 1)
+  uint64_t terms_n = 0, pterms_n = 0, ppos_n = 0;  // positions in terms and pterms, parents in ppos
+  unsigned long long* chk = nullptr;               // bounds record
   bool scale = true;               // some integral of the run has a box other than the unit cube
 };
 
@@ -419,8 +438,8 @@ inline cudaError_t launch_setsum_shape(const pg_eval_args& a, const SegDesc* seg
   if (g > 0x7fffffffull) return cudaErrorInvalidValue;
   setsum_kernel<MAXD, SCALE><<<(unsigned)g, kSetSumThreads, smem, (cudaStream_t)a.stream>>>(
       a.left, a.length, a.n, a.stride, a.owner, static_cast<const IntegralDesc*>(a.descs),
-      *static_cast<const RuleDev*>(a.rule), a.est, a.err, a.bisect, segs, base, c.pcache, c.pcache_rows, c.terms,
-      c.terms_rows);
+      *static_cast<const RuleDev*>(a.rule), a.est, a.err, a.bisect, segs, base, c.pterms, c.ppos, c.terms,
+      c.terms_rows, c.terms_n, c.pterms_n, c.ppos_n, c.chk);
   return cudaGetLastError();
 }
 

@@ -78,3 +78,17 @@ def test_high_dimensions_bitwise(ctx, orc, d):
     r = ctx.integrate(f, 1e-3, 0.0)
     o, _ = orc.integrate(f, 1e-3, 0.0)
     assert _same(r, o)
+
+
+def test_heuristic_classifier_in_a_batch(ctx, orc):
+    """Several integrals run the classifier's threshold search in the same
+    iterations (a small memory model): each result equals the oracle's alone."""
+    rng = np.random.default_rng(21)
+    fs = [pg.genz(pg.PRODUCT_PEAK, rng.random(d) * 8 + 2, rng.random(d)) for d in (3, 4, 5, 5, 6)]
+    opt = pg.default_options(device_mem_model=2e6)
+    batch = ctx.batch_integrate(fs, [1e-7] * len(fs), 0.0, options=opt)
+    for f, b in zip(fs, batch):
+        o, _ = orc.integrate(f, 1e-7, 0.0, device_mem=2e6)
+        assert _same(b, o)
+    st = ctx.stats()
+    assert st.classify_passes > 0
