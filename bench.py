@@ -160,10 +160,10 @@ def load_screen():
 # The driver's peak file holds HBM and bf16 figures only.  A libm call or a
 # division counts the FP64 instructions it executes on this GPU, measured by
 # ncu (smsp__sass_thread_inst_executed_op_fp64_pred_on per region, less the
-# counted arithmetic: profiles/setsum_kernel_fp64_mix.md).  The set-sum
-# kernel's multiplies run on the FP64 pipe and are counted; the point-by-point
-# kernel's products of the point values run on the integer pipe
-# (pg::mul_rn_int) and are not.
+# counted arithmetic: profiles/setsum_kernel_fp64_mix.md).  Multiplies that
+# run on the integer pipe (pg::mul_rn_int) are not counted: the point-by-point
+# kernel's products of the point values and the set-sum kernel's products of
+# the fourth differences' point values.
 LIBM_OPS = {"exp": 17.2, "div": 6.2, "cos": 22.0}
 
 
@@ -176,30 +176,20 @@ def _factor_ops(family):
             pg.PRODUCT: 0}.get(family, 0)
 
 
-def _fd_products(d):
-    """Multiplies of the fourth differences' point values (two half products per point)."""
-    m = d // 2
-    n = (m - 1) + (d - m - 1) + 1            # the centre's half products and L * R
-    for k in range(d):
-        hbeg, hend = (0, m) if k < m else (m, d)
-        n += 4 * (k != hbeg) + 4 * (hend - k - 1) + 4 + (k != hbeg)
-    return n
-
-
 def setsum_ops(family, d, unit=True, paired=0.0, cached=0.0):
     """FP64 operations per region of setsum_kernel (PG_EVAL_SET_SUMS).  An evaluated axis
     costs 11 coordinates (a multiply and an FMA, one more off the unit cube), 11 factors and
     5 pair sums; a step of the set-sum recurrence 8 FMAs and 9 multiplies; a region's tail
-    40 rule-sum FMAs and 5 multiplies, the fourth differences (5 d + 1, and the products of
-    their point values), 27 null-rule FMAs and 27 multiplies, and 10 more (volume, error
-    ladder, results).  A region alone evaluates d axes and d steps.  A sibling pair
+    40 rule-sum FMAs and 5 multiplies, the fourth differences (5 d + 1; the products of
+    their point values run on the integer pipe), 27 null-rule FMAs and 27 multiplies, and
+    10 more (volume, error ladder, results).  A region alone evaluates d axes and d steps.  A sibling pair
     evaluates d + 1 axes (the second sibling's split axis only) and d + 1 steps (d - 1
     shared); a pair whose parent's terms are kept evaluates the split axis of each sibling
     and adds 2 sums for every other axis.  `paired`: the share of regions evaluated in
     pairs; `cached`: the share of pairs with their parent's terms."""
     axis = 11 * (2 if unit else 3) + 11 * _factor_ops(family) + 5
     step = 8 + 9
-    tail = 45 + (5 * d + 1) + _fd_products(d) + 54 + (d - 1) + 10
+    tail = 45 + (5 * d + 1) + 54 + (d - 1) + 10
     alone = d * (axis + step) + tail
     pair = (d + 1) * axis + (d + 1) * step + 2 * tail
     pair_cached = 2 * axis + 2 * (d - 1) + (d + 1) * step + 2 * tail

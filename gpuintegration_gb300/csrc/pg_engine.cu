@@ -398,9 +398,11 @@ int Engine::threshold_pass(uint32_t jidx, double thr, int write_flags, int minma
                            bool readback) {
   const SegDesc& S = ((const SegDesc*)h_segs_.p)[jidx];
   if (S.nchunks) {
-    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(
-        (const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, S.chunk_start, (const double*)est_.p,
-        (const double*)err_b_.p, thr, nullptr, write_flags, minmax, (uint8_t*)active_.p, (Partial*)partials_.p);
+    // the sums are read only from a pass that neither writes flags nor takes extremes
+    auto kern = (!write_flags && !minmax) ? threshold_kernel<true> : threshold_kernel<false>;
+    kern<<<S.nchunks, kRedThreads, 0, stream_>>>((const ChunkRef*)chunks_.p, (const SegDesc*)segs_.p, S.chunk_start,
+                                                 (const double*)est_.p, (const double*)err_b_.p, thr, nullptr,
+                                                 write_flags, minmax, (uint8_t*)active_.p, (Partial*)partials_.p);
     stats.launches++;
   }
   threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>((const SegDesc*)segs_.p, jidx,
@@ -463,9 +465,9 @@ int Engine::classify_chain(uint32_t jidx, double thr0, double pct, uint64_t n) {
   ThresholdSet none;
   std::memset(&none, 0, sizeof none);
   if (S.nchunks) {
-    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)est_.p,
-                                                             (const double*)err_b_.p, INFINITY, nullptr, 0, 1,
-                                                             (uint8_t*)active_.p, (Partial*)partials_.p);
+    threshold_kernel<false><<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)est_.p,
+                                                                    (const double*)err_b_.p, INFINITY, nullptr, 0,
+                                                                    1, (uint8_t*)active_.p, (Partial*)partials_.p);
     stats.launches++;
   }
   threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>(sg, jidx, (const Partial*)partials_.p,
@@ -479,9 +481,9 @@ int Engine::classify_chain(uint32_t jidx, double thr0, double pct, uint64_t n) {
   }
   threshold_select_kernel<<<1, 32, 0, stream_>>>(cnt, cb + 40, n, pct, cb + 60);
   if (S.nchunks) {
-    threshold_kernel<<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)est_.p,
-                                                             (const double*)err_b_.p, 0.0, cb + 60, 0, 0,
-                                                             (uint8_t*)active_.p, (Partial*)partials_.p);
+    threshold_kernel<true><<<S.nchunks, kRedThreads, 0, stream_>>>(ch, sg, S.chunk_start, (const double*)est_.p,
+                                                                   (const double*)err_b_.p, 0.0, cb + 60, 0, 0,
+                                                                   (uint8_t*)active_.p, (Partial*)partials_.p);
     stats.launches++;
   }
   threshold_finalize_kernel<<<1, kRedThreads, 0, stream_>>>(sg, jidx, (const Partial*)partials_.p,

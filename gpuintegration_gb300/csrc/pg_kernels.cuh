@@ -336,8 +336,12 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
 // Memory-pressure classifier support (heuristic_classifier.cuh:60-87,283-325):
 // per chunk of one integral, count(err > thr), sum(err * flag), sum(est * flag)
 // and (optionally) the new flags.  Partial.q[0] = err*flag, q[1] = est*flag,
-// q[2] = min(err) in .s, max(err) in .c (when `minmax`).
+// q[2] = min(err) in .s, max(err) in .c (when `minmax`).  Without SUMS the
+// compensated sums are left out (zero): the min/max pass and the pass that
+// writes the final flags read only counts and extremes, and the sums cost
+// ~12 FP64 operations per region on the scarce FP64 pipe.
 // ---------------------------------------------------------------------------
+template <bool SUMS>
 static __global__ void __launch_bounds__(kRedThreads)
     threshold_kernel(const ChunkRef* __restrict__ chunks, const SegDesc* __restrict__ segs, uint32_t chunk0,
                      const double* __restrict__ est, const double* __restrict__ err, double thr_arg,
@@ -362,8 +366,10 @@ static __global__ void __launch_bounds__(kRedThreads)
       const uint8_t f = e > thr ? 1 : 0;
       const double ff = f ? 1.0 : 0.0;
       if (write_flags) active[i] = f;
-      a0 = ns_merge(a0, NS{__dmul_rn(e, ff), 0.0});
-      a1 = ns_merge(a1, NS{__dmul_rn(est[i], ff), 0.0});
+      if (SUMS) {
+        a0 = ns_merge(a0, NS{__dmul_rn(e, ff), 0.0});
+        a1 = ns_merge(a1, NS{__dmul_rn(est[i], ff), 0.0});
+      }
       cnt += f;
       if (minmax && !isnan(e)) {
         mn = fmin(mn, e);
@@ -371,25 +377,30 @@ static __global__ void __launch_bounds__(kRedThreads)
       }
     }
   }
-  a0 = ns_block_tree(a0, scratch);
-  a1 = ns_block_tree(a1, scratch);
+  if (SUMS) {
+    a0 = ns_block_tree(a0, scratch);
+    a1 = ns_block_tree(a1, scratch);
+  }
   atomicAdd(&cnt_s, (unsigned long long)cnt);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (minmax) {
 #pragma unroll
-  for (int off = 16; off >= 1; off >>= 1) {
-    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, off));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-  }
-  if (lane == 0) {
-    mm[0][warp] = mn;
-    mm[1][warp] = mx;
+    for (int off = 16; off >= 1; off >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) {
+      mm[0][warp] = mn;
+      mm[1][warp] = mx;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 0; w < 8; ++w) {
-      mn = fmin(mn, mm[0][w]);
-      mx = fmax(mx, mm[1][w]);
-    }
+    if (minmax)
+      for (int w = 0; w < 8; ++w) {
+        mn = fmin(mn, mm[0][w]);
+        mx = fmax(mx, mm[1][w]);
+      }
     Partial& P = partials[chunk0 + blockIdx.x];
     P.q[0] = a0;
     P.q[1] = a1;

@@ -68,13 +68,24 @@
 
 namespace pg {
 
-// Multiplies of the set-sum kernel: on the FP64 pipe (__dmul_rn), or with
-// -DPG_SETSUM_MUL=mul_rn_int on the integer pipe; the same bits either way.
-// (With the parents' terms kept, the FP64 pipe has room for them: on GB300
-// the FP64 form is 10-18% faster on 8-D integrals and as fast on the batched
-// workload.)
+// Multiplies of the set-sum kernel, each site on the FP64 pipe (__dmul_rn) or
+// on the integer pipe (pg::mul_rn_int), the same bits either way.  The kernel
+// is FP64-bound, so the split balances the two pipes: measured on GB300, the
+// fourth differences' point products (117 per 8-D region) on the integer pipe
+// and the rest on the FP64 pipe is 11% faster on the batched workload than
+// all on the FP64 pipe, which is itself 10-18% faster than all on the integer
+// pipe on 8-D integrals.
 #ifndef PG_SETSUM_MUL
 #define PG_SETSUM_MUL __dmul_rn
+#endif
+#ifndef PG_SETSUM_MUL_FD
+#define PG_SETSUM_MUL_FD mul_rn_int  // the fourth differences' point products
+#endif
+#ifndef PG_SETSUM_MUL_NULL
+#define PG_SETSUM_MUL_NULL PG_SETSUM_MUL  // the null rules' scaled terms
+#endif
+#ifndef PG_SETSUM_MUL_STEP
+#define PG_SETSUM_MUL_STEP PG_SETSUM_MUL  // the set-sum recurrence
 #endif
 
 constexpr int kSetSumThreads = 128;
@@ -102,15 +113,15 @@ struct SetSums {
 };
 
 __device__ __forceinline__ void set_step(SetSums& S, const AxisTerm& A) {
-  S.t3 = __fma_rn(S.b, A.p0, PG_SETSUM_MUL(S.t3, A.c));
-  S.g = __fma_rn(S.a1, A.p0, __fma_rn(S.a0, A.p1, PG_SETSUM_MUL(S.g, A.c)));
-  S.b = __fma_rn(S.a0, A.p0, PG_SETSUM_MUL(S.b, A.c));
-  S.a0 = __fma_rn(S.e0, A.p0, PG_SETSUM_MUL(S.a0, A.c));
-  S.a1 = __fma_rn(S.e0, A.p1, PG_SETSUM_MUL(S.a1, A.c));
-  S.a2 = __fma_rn(S.e0, A.p2, PG_SETSUM_MUL(S.a2, A.c));
-  S.a3 = __fma_rn(S.e0, A.p3, PG_SETSUM_MUL(S.a3, A.c));
-  S.e0 = PG_SETSUM_MUL(S.e0, A.c);
-  S.z = PG_SETSUM_MUL(S.z, A.p4);
+  S.t3 = __fma_rn(S.b, A.p0, PG_SETSUM_MUL_STEP(S.t3, A.c));
+  S.g = __fma_rn(S.a1, A.p0, __fma_rn(S.a0, A.p1, PG_SETSUM_MUL_STEP(S.g, A.c)));
+  S.b = __fma_rn(S.a0, A.p0, PG_SETSUM_MUL_STEP(S.b, A.c));
+  S.a0 = __fma_rn(S.e0, A.p0, PG_SETSUM_MUL_STEP(S.a0, A.c));
+  S.a1 = __fma_rn(S.e0, A.p1, PG_SETSUM_MUL_STEP(S.a1, A.c));
+  S.a2 = __fma_rn(S.e0, A.p2, PG_SETSUM_MUL_STEP(S.a2, A.c));
+  S.a3 = __fma_rn(S.e0, A.p3, PG_SETSUM_MUL_STEP(S.a3, A.c));
+  S.e0 = PG_SETSUM_MUL_STEP(S.e0, A.c);
+  S.z = PG_SETSUM_MUL_STEP(S.z, A.p4);
 }
 
 // The 11 factor values of axis k over [lo, up] (coordinates as Sample.cuh:126-131
@@ -189,10 +200,10 @@ __device__ __forceinline__ int region_result(const SetSumSmem<MAXD>& Sm, const R
   // evaluation forms them: L * R from the two half products in axis order.
   const int m = d / 2;
   double Lc = F(0, 0), Rc = F(m, 0);
-  for (int k = 1; k < m; ++k) Lc = PG_SETSUM_MUL(Lc, F(k, 0));
-  for (int k = m + 1; k < d; ++k) Rc = PG_SETSUM_MUL(Rc, F(k, 0));
-  double f0 = PG_SETSUM_MUL(Lc, Rc);
-  if (scale_jac) f0 = PG_SETSUM_MUL(f0, jac);
+  for (int k = 1; k < m; ++k) Lc = PG_SETSUM_MUL_FD(Lc, F(k, 0));
+  for (int k = m + 1; k < d; ++k) Rc = PG_SETSUM_MUL_FD(Rc, F(k, 0));
+  double f0 = PG_SETSUM_MUL_FD(Lc, Rc);
+  if (scale_jac) f0 = PG_SETSUM_MUL_FD(f0, jac);
   const double f02 = __dadd_rn(f0, f0);
   unsigned long long kmax = 0ull;
   int cand = -1;
@@ -203,20 +214,20 @@ __device__ __forceinline__ int region_result(const SetSumSmem<MAXD>& Sm, const R
     // The half product of each of the four points, the four chains side by side.
     double f[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) f[v] = (k == hbeg) ? F(k, 1 + v) : PG_SETSUM_MUL(pre, F(k, 1 + v));
+    for (int v = 0; v < 4; ++v) f[v] = (k == hbeg) ? F(k, 1 + v) : PG_SETSUM_MUL_FD(pre, F(k, 1 + v));
     for (int q = k + 1; q < hend; ++q) {
       const double cq = F(q, 0);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) f[v] = PG_SETSUM_MUL(f[v], cq);
+      for (int v = 0; v < 4; ++v) f[v] = PG_SETSUM_MUL_FD(f[v], cq);
     }
     const double other = lhalf ? Rc : Lc;  // the other half's centre product
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      f[v] = PG_SETSUM_MUL(f[v], other);
-      if (scale_jac) f[v] = PG_SETSUM_MUL(f[v], jac);
+      f[v] = PG_SETSUM_MUL_FD(f[v], other);
+      if (scale_jac) f[v] = PG_SETSUM_MUL_FD(f[v], jac);
     }
     const double ck = F(k, 0);
-    pre = (k == hbeg) ? ck : PG_SETSUM_MUL(pre, ck);
+    pre = (k == hbeg) ? ck : PG_SETSUM_MUL_FD(pre, ck);
     if (k + 1 == m) pre = 1.0;
     // base + ratio*(fp+fm) - (fp2+fm2), base = 2*f0*(1-ratio): the
     // reference's compiled code fuses the base multiply for d <= 4 and the
@@ -243,7 +254,7 @@ __device__ __forceinline__ int region_result(const SetSumSmem<MAXD>& Sm, const R
 #pragma unroll
     for (int q = 1; q <= 3; ++q) {
       const unsigned long long bt = (unsigned long long)__double_as_longlong(
-          PG_SETSUM_MUL(fabs(__fma_rn(SC[st * kNRules + q], s5[q], s5[q + 1])), NM[st * kNRules + q]));
+          PG_SETSUM_MUL_NULL(fabs(__fma_rn(SC[st * kNRules + q], s5[q], s5[q + 1])), NM[st * kNRules + q]));
       const unsigned long long term = (bt & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : bt;
       mq[q - 1] = term > mq[q - 1] ? term : mq[q - 1];
     }
