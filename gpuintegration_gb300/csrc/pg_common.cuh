@@ -116,9 +116,13 @@ __host__ __device__ inline NS ns_zero() { return NS{0.0, 0.0}; }
 
 // merge(a, b): t = a.s + b.s; the rounding error of that addition goes into
 // the correction term; value = s + c.
+// The larger-magnitude operand is selected first, so the error term costs two
+// FP64 additions rather than both branches' four.
 __device__ __forceinline__ NS ns_merge(NS a, NS b) {
   const double t = __dadd_rn(a.s, b.s);
-  const double e = (fabs(a.s) >= fabs(b.s)) ? __dadd_rn(__dadd_rn(a.s, -t), b.s) : __dadd_rn(__dadd_rn(b.s, -t), a.s);
+  const bool ge = fabs(a.s) >= fabs(b.s);
+  const double big = ge ? a.s : b.s, small = ge ? b.s : a.s;
+  const double e = __dadd_rn(__dadd_rn(big, -t), small);
   return NS{t, __dadd_rn(__dadd_rn(a.c, b.c), e)};
 }
 
