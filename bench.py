@@ -287,6 +287,17 @@ def run_mcubes(args):
             "estimate": r.estimate, "errorest": r.errorest, "sigma_from_1": (r.estimate - 1.0) / r.errorest,
             "iters": r.iters, "status": r.status, "samples_per_s": r.neval / el,
             "same_seed_bitwise": (key(first) == key(r)) if args.warmup else None}
+    # CPU baseline: the oracle's m-Cubes restatement (one host thread) on a bounded sample of the same
+    # integrand (ncall 2^20, 3 iterations), its sampling rate applied to this run's samples.
+    from oracle import oracle as orc
+    t0 = time.perf_counter()
+    o, _ = orc.mcubes_integrate(f, 1e-4, 0.0, 2.0 ** 20, titer=3, itmax=3, skip=5, seed=2024)
+    cpu_s = time.perf_counter() - t0
+    rate = o.neval / cpu_s
+    line["cpu_baseline"] = {"value": 1000.0 * r.neval / rate, "unit": "ms", "cores": 1, "kind": "port",
+                            "samples_per_s": rate,
+                            "sample": f"ncall 2^20 x 3 iterations ({o.neval} samples, {cpu_s:.1f} s), time to "
+                                      f"solution extrapolated to this run's {r.neval} samples"}
     print(json.dumps(line), flush=True)
 
 
