@@ -157,7 +157,7 @@ def load_screen():
 # whether FMA, multiply or add), so their work is counted in FP64 operations
 # per region of each kernel's algorithm, and the peak is this GPU's FP64
 # instruction rate, measured by pg_probe_fp64_peak (an FMA loop; TFLOP/s / 2).
-# The driver's peak file holds HBM and bf16 figures only.  A libm call or a
+# The measured-peaks file holds HBM and bf16 figures only.  A libm call or a
 # division counts the FP64 instructions it executes on this GPU, measured by
 # ncu (smsp__sass_thread_inst_executed_op_fp64_pred_on per region, less the
 # counted arithmetic: profiles/setsum_kernel_fp64_mix.md).  Multiplies that

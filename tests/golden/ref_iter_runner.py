@@ -12,7 +12,7 @@ The host loop around them restates Workspace::integrate
 (PaganiUtils.cuh:387-394), compute_finished_estimates (PaganiUtils.cuh:368-385),
 fix_error_budget_overflow (Workspace.cuh:121-146), the heuristic classifier's
 trigger (Workspace.cuh:74-118, heuristic_classifier.cuh:89-145,349-360; the
-cases used never reach it, and the driver refuses to run one that would), the
+cases used never reach it, and this runner refuses to run one that would), the
 exclusive scan and active count of Sub_region_filter.cuh:61-82, and the
 iteration cap of 700.  Sums use numpy's order; the reference's thrust::reduce
 order is unspecified, so iteration totals may differ from a real run in the
