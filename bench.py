@@ -151,6 +151,15 @@ def load_screen():
     return json.load(open(SCREEN))
 
 
+def _oracle_checked(screen):
+    """The screen's oracle re-check (tests/golden/make_config4_screen.py --oracle-check), in words."""
+    oc = screen.get("oracle_check")
+    if not oc:
+        return "no candidate (not run)"
+    return (f"{oc['accepted_agree']} of {oc['accepted_checked']} light accepted and "
+            f"{oc['rejected_agree']} of {oc['rejected_checked']} low-dimension rejected candidates")
+
+
 # ---------------------------------------------------------------------------
 # Roofline of region evaluation.  The kernels are bound by the FP64 pipe
 # (GB300: 2 FP64 lanes per SM per clock, one pipe slot per FP64 instruction
@@ -592,7 +601,8 @@ def run_batched(args, rank, world, local, t_begin):
                        "eval_mode": args.eval_mode,
                        "screen": f"{len(screen['accepted'])} of the first {screen['accepted'][-1] + 1} candidates "
                                  f"converge within tolerance (unscreened pass rate "
-                                 f"{len(screen['accepted']) / (screen['accepted'][-1] + 1):.3f})"},
+                                 f"{len(screen['accepted']) / (screen['accepted'][-1] + 1):.3f}); the CPU oracle "
+                                 f"repeats the decision on {_oracle_checked(screen)}"},
             "e2e": {"value": e2e, "unit": "integrals/s", "h2d_bytes_per_step": st.h2d_bytes // args.steps,
                     "d2h_bytes_per_step": st.d2h_bytes // args.steps},
             "gpu_launches": int(st.launches), "clocks": clk,

@@ -9,7 +9,14 @@ per-integral results are those of its plain path (tests/test_gpu_batch.py),
 which matches the CPU oracle (bit-identical for integrands built from
 + - * /; tests/test_gpu_parity.py, tests/test_gpu_config2.py).
 
-Writes tests/golden/config4_screen.json.  Needs a GPU.
+`python make_config4_screen.py` (needs a GPU) writes
+tests/golden/config4_screen.json.  `python make_config4_screen.py
+--oracle-check` (CPU only) repeats the screen's decision with the CPU oracle on
+every candidate the oracle finishes in well under a second -- the accepted
+candidates with at most ORACLE_MAX_REGIONS regions and the rejected
+candidates of dimension at most ORACLE_MAX_REJECTED_DIM -- and records the
+agreement in the file's `oracle_check` entry (tests/test_config4_screen.py
+repeats a seeded sample of it).
 """
 import json
 import os
@@ -17,13 +24,18 @@ import sys
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
 
-import gpuintegration_gb300 as pg  # noqa: E402
 from gpuintegration_gb300 import workloads as W  # noqa: E402
+
+PATH = os.path.join(HERE, "config4_screen.json")
+ORACLE_MAX_REGIONS = 20000
+ORACLE_MAX_REJECTED_DIM = 5
 
 
 def main(target=4096, candidates=5600, master=4096):
+    import gpuintegration_gb300 as pg
     cases = W.mixed_cases(candidates, master, 2, 8, 1e-7, 1e-4)
     ctx = pg.Context(0)
     t0 = time.time()
@@ -45,10 +57,56 @@ def main(target=4096, candidates=5600, master=4096):
         "nregions": [int(res[i].nregions) for i in accepted],
         "neval": [int(res[i].neval) for i in accepted],
     }
-    with open(os.path.join(HERE, "config4_screen.json"), "w") as f:
+    with open(PATH, "w") as f:
         json.dump(out, f, separators=(",", ":"))
     print(f"accepted {target} of {last + 1} candidates ({len(out['rejected_before_last'])} rejected) in {elapsed:.1f}s")
 
 
+def candidates_of(screen):
+    """The candidate stream up to the last accepted candidate."""
+    return W.mixed_cases(screen["accepted"][-1] + 1, screen["master"], screen["dmin"], screen["dmax"],
+                         screen["eps_lo"], screen["eps_hi"])
+
+
+def oracle_decision(oracle, case, threads=None):
+    """(accepted, result) of the CPU oracle on one candidate: status 0 and within epsrel of the exact value."""
+    r, _ = oracle.integrate(case.integrand, case.epsrel, 0.0, nthreads=threads)
+    return r.status == 0 and W.within_tolerance(r.estimate, case.exact, case.epsrel), r
+
+
+def oracle_check():
+    from oracle import oracle
+    oracle.load()
+    screen = json.load(open(PATH))
+    cand = candidates_of(screen)
+    t0 = time.time()
+    acc_n = acc_ok = 0
+    for k, i in enumerate(screen["accepted"]):
+        if screen["nregions"][k] > ORACLE_MAX_REGIONS:
+            continue
+        ok, r = oracle_decision(oracle, cand[i])
+        acc_n += 1
+        acc_ok += ok and r.nregions == screen["nregions"][k] and r.neval == screen["neval"][k]
+    rej_n = rej_ok = 0
+    for i in screen["rejected_before_last"]:
+        if cand[i].integrand.ndim > ORACLE_MAX_REJECTED_DIM:
+            continue
+        ok, _ = oracle_decision(oracle, cand[i])
+        rej_n += 1
+        rej_ok += not ok
+    screen["oracle_check"] = {
+        "accepted_checked": acc_n, "accepted_agree": acc_ok, "rejected_checked": rej_n, "rejected_agree": rej_ok,
+        "rule": f"CPU oracle on every accepted candidate with <= {ORACLE_MAX_REGIONS} regions (same decision, "
+                f"region and evaluation counts) and every rejected candidate of dimension <= "
+                f"{ORACLE_MAX_REJECTED_DIM} (rejected too)",
+        "seconds": round(time.time() - t0, 1)}
+    with open(PATH, "w") as f:
+        json.dump(screen, f, separators=(",", ":"))
+    print(json.dumps(screen["oracle_check"]))
+
+
 if __name__ == "__main__":
-    main()
+    if "--oracle-check" in sys.argv[1:]:
+        oracle_check()
+    else:
+        main()
