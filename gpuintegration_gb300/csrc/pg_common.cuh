@@ -114,16 +114,36 @@ struct NS {
 
 __host__ __device__ inline NS ns_zero() { return NS{0.0, 0.0}; }
 
+// |a| >= |b| on the integer pipe: for doubles that are not NaN, the order of
+// the bit patterns with the sign bit cleared is the order of the magnitudes.
+// (With a NaN operand the sum is NaN whichever operand is taken as larger.)
+__device__ __forceinline__ bool mag_ge(double a, double b) {
+  const unsigned long long m = 0x7fffffffffffffffull;
+  return ((unsigned long long)__double_as_longlong(a) & m) >= ((unsigned long long)__double_as_longlong(b) & m);
+}
+
 // merge(a, b): t = a.s + b.s; the rounding error of that addition goes into
 // the correction term; value = s + c.
-// The larger-magnitude operand is selected first, so the error term costs two
-// FP64 additions rather than both branches' four.
+// The larger-magnitude operand is selected first (compared on the integer
+// pipe), so the error term costs two FP64 additions rather than both
+// branches' four.
 __device__ __forceinline__ NS ns_merge(NS a, NS b) {
   const double t = __dadd_rn(a.s, b.s);
-  const bool ge = fabs(a.s) >= fabs(b.s);
+  const bool ge = mag_ge(a.s, b.s);
   const double big = ge ? a.s : b.s, small = ge ? b.s : a.s;
   const double e = __dadd_rn(__dadd_rn(big, -t), small);
   return NS{t, __dadd_rn(__dadd_rn(a.c, b.c), e)};
+}
+
+// ns_merge(a, NS{x, 0.0}) with one addition fewer, bit for bit: a correction
+// term is never -0.0 (it starts at +0.0, and an exact zero sum rounds to
+// +0.0), so a.c + 0.0 is a.c.
+__device__ __forceinline__ NS ns_add(NS a, double x) {
+  const double t = __dadd_rn(a.s, x);
+  const bool ge = mag_ge(a.s, x);
+  const double big = ge ? a.s : x, small = ge ? x : a.s;
+  const double e = __dadd_rn(__dadd_rn(big, -t), small);
+  return NS{t, __dadd_rn(a.c, e)};
 }
 
 __device__ __forceinline__ NS ns_shfl_down(NS v, int off) {

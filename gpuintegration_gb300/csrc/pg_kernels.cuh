@@ -146,10 +146,10 @@ static __global__ void __launch_bounds__(kRedThreads)
       err_out[i] = selfErr;
       active[i] = act;
       const double fa = act ? 1.0 : 0.0;
-      a0 = ns_merge(a0, NS{selfRes, 0.0});
-      a1 = ns_merge(a1, NS{selfErr, 0.0});
-      a2 = ns_merge(a2, NS{__dmul_rn(fa, selfRes), 0.0});
-      a3 = ns_merge(a3, NS{__dmul_rn(fa, selfErr), 0.0});
+      a0 = ns_add(a0, selfRes);
+      a1 = ns_add(a1, selfErr);
+      a2 = ns_add(a2, __dmul_rn(fa, selfRes));
+      a3 = ns_add(a3, __dmul_rn(fa, selfErr));
       cnt += act;
     }
   }
@@ -339,7 +339,7 @@ static __global__ void __launch_bounds__(kRedThreads, 3)
 // q[2] = min(err) in .s, max(err) in .c (when `minmax`).  Without SUMS the
 // compensated sums are left out (zero): the min/max pass and the pass that
 // writes the final flags read only counts and extremes, and the sums cost
-// ~12 FP64 operations per region on the scarce FP64 pipe.
+// ~10 FP64 operations per region on the scarce FP64 pipe.
 // ---------------------------------------------------------------------------
 template <bool SUMS>
 static __global__ void __launch_bounds__(kRedThreads)
@@ -367,8 +367,8 @@ static __global__ void __launch_bounds__(kRedThreads)
       const double ff = f ? 1.0 : 0.0;
       if (write_flags) active[i] = f;
       if (SUMS) {
-        a0 = ns_merge(a0, NS{__dmul_rn(e, ff), 0.0});
-        a1 = ns_merge(a1, NS{__dmul_rn(est[i], ff), 0.0});
+        a0 = ns_add(a0, __dmul_rn(e, ff));
+        a1 = ns_add(a1, __dmul_rn(est[i], ff));
       }
       cnt += f;
       if (minmax && !isnan(e)) {
@@ -562,7 +562,7 @@ static __global__ void __launch_bounds__(kRedThreads) sum_chunks_kernel(const do
 #pragma unroll
   for (int k = 0; k < kRedItems; ++k) {
     const uint64_t i = (uint64_t)blockIdx.x * kChunk + (uint64_t)k * kRedThreads + threadIdx.x;
-    if (i < n) a = ns_merge(a, NS{x[i], 0.0});
+    if (i < n) a = ns_add(a, x[i]);
   }
   a = ns_block_tree(a, scratch);
   if (threadIdx.x == 0) part[blockIdx.x] = a;

@@ -96,27 +96,40 @@ def _reference_tree():
     return ref if os.path.isfile(os.path.join(ref, "common", "cuda", "Interp1D.cuh")) else None
 
 
-def test_reference_helpers_compile_in_functors():
-    """Functors built on the reference's Interp1D/2D/3D and cudaDynamicArray
-    (test/cuda/common/StatefulIntegrand.cu:34-97) compile against the C++
-    layer.  Needs the reference tree (REF); skipped without it."""
+@pytest.mark.parametrize("helpers_first", [0, 1])
+def test_reference_helpers_compile_in_functors(helpers_first):
+    """Functors built on the reference's Interp1D/2D/3D, polynomial and
+    cudaDynamicArray (test/cuda/common/StatefulIntegrand.cu:34-97) compile
+    against the C++ layer, with this library's helpers header included before
+    or after the reference's.  Needs the reference tree (REF); skipped without it."""
     ref = _reference_tree()
     if ref is None:
         pytest.skip("reference tree not present")
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(ROOT, "tests", "cpp", "ref_helpers_check.cu")
-    out = os.path.join(BUILD, "ref_helpers_check.o")
-    subprocess.check_call([_nvcc()] + _flags() + ["-I" + ref, "-I" + os.path.join(ref, "externals"), "-c", src,
-                                                  "-o", out])
+    out = os.path.join(BUILD, f"ref_helpers_check_{helpers_first}.o")
+    subprocess.check_call([_nvcc()] + _flags() + ["-I" + ref, "-I" + os.path.join(ref, "externals"),
+                                                  f"-DHELPERS_FIRST={helpers_first}", "-c", src, "-o", out])
+    assert os.path.getsize(out) > 0
+
+
+def test_helpers_header_compiles():
+    """include/pagani_gb300_helpers.cuh with the C++ layer: the GPU check program compiles (no GPU needed)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "helpers_check.cu")
+    out = os.path.join(BUILD, "helpers_check.o")
+    subprocess.check_call([_nvcc()] + _flags() + ["-c", src, "-o", out])
     assert os.path.getsize(out) > 0
 
 
 @pytest.mark.gpu
 def test_stateful_helper_functors_run(lib):
-    """Functors of the helpers' shapes (a deep-copying managed array; 1-D and
-    2-D interpolation tables) through Workspace::integrate, against their
-    exact integrals; the non-trivially-copyable functor reaches the kernel as
-    a managed copy."""
+    """The library's integrand-side helpers (include/pagani_gb300_helpers.cuh):
+    the reference's known answers for Interp1D/2D/3D, cudaDynamicArray and
+    stateful integrands; device equals host bit for bit and agrees with the
+    reference's interpolation formulas to 1e-14; functors holding them through
+    Workspace::integrate against exact integrals; table copies share one
+    device store."""
     from gpuintegration_gb300 import _build
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(ROOT, "tests", "cpp", "helpers_check.cu")
@@ -130,5 +143,12 @@ def test_stateful_helper_functors_run(lib):
     assert p.returncode == 0, p.stdout + p.stderr
     assert lines and lines[-1].startswith("DONE 0 failures")
     names = {ln.split()[1] for ln in lines if ln.startswith("PASS")}
-    for case in ("heap_model2", "heap_model2_managed_copy", "interp1d_3", "interp2d_4"):
+    for case in ("ref_interp1d_exact_at_knots", "ref_interp1d_quadratic", "ref_interp2d_value", "ref_interp2d_clamp",
+                 "ref_interp2d_exact_at_knots", "ref_interp2d_bilinear", "ref_interp3d_linear",
+                 "ref_interp3d_quadratic", "ref_interp3d_clamp", "ref_dynamic_array", "dynamic_array_device_copy",
+                 "ref_stateful_array", "ref_stateful_dynamic_array", "interp1d_device_equals_host",
+                 "interp1d_vs_reference_formula", "interp2d_device_equals_host", "interp2d_vs_reference_formula",
+                 "interp3d_device_equals_host", "interp3d_vs_reference_formula", "polynomial_device_equals_host",
+                 "polynomial_vs_horner", "interp_stream_input", "interp_rejects_unordered_axis", "interp1d_3",
+                 "interp2d_4", "interp3d_3", "polynomial_dynamic_array_2", "interp_copies_share_device_store"):
         assert case in names, case
