@@ -174,6 +174,20 @@ def _oracle_checked(screen):
 # kernel's products of the point values and the set-sum kernel's products of
 # the fourth differences' point values.
 LIBM_OPS = {"exp": 17.2, "div": 6.2, "cos": 22.0}
+# ncu's FP64-pipe utilisation of setsum_kernel (sm__pipe_fp64_cycles_active over
+# 152 SMs x elapsed cycles), from profiles/setsum_kernel_fp64_mix.md: the
+# counter-side view of the same roofline.
+NCU_FP64_PIPE_ACTIVE = {"cached_sibling_pairs_c0_8d": 0.699, "lone_regions_c0_8d": 0.833,
+                        "source": "profiles/setsum_kernel_fp64_mix.md"}
+
+
+def _hbm_frac(gbs):
+    """Evaluation DRAM GB/s over the measured copy bandwidth (MEASURED_PEAKS.json), when that file is present."""
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        return None
+    return gbs / peak
 
 
 def _factor_ops(family):
@@ -515,7 +529,9 @@ def roofline(ctx, cases, results, st, steps, mode):
             "algorithmic_bytes_per_launch": alg_bytes,
             "traffic_note": "algorithmic bytes x the DRAM/algorithmic ratio ncu measured on a 1M-region 8-D "
                             "setsum_kernel launch",
-            "hbm_gbs_of_eval": st.eval_bytes / eval_s / 1e9}
+            "hbm_gbs_of_eval": st.eval_bytes / eval_s / 1e9,
+            "hbm_frac_of_measured": _hbm_frac(st.eval_bytes / eval_s / 1e9),
+            "ncu_fp64_pipe_active": NCU_FP64_PIPE_ACTIVE}
 
 
 def iteration_summary(it, steps):
