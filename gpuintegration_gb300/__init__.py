@@ -43,11 +43,12 @@ PG_UNSUPPORTED = -5
 EVAL_POINTS = 0
 EVAL_SET_SUMS = 1
 
-CONSTANT, OSCILLATORY, PRODUCT_PEAK, CORNER_PEAK, GAUSSIAN, C0, DISCONTINUOUS, PRODUCT, NAN_VALUE, BOX, FUN6 = range(11)
+(CONSTANT, OSCILLATORY, PRODUCT_PEAK, CORNER_PEAK, GAUSSIAN, C0, DISCONTINUOUS, PRODUCT, NAN_VALUE, BOX, FUN6,
+ GAUSSIAN_SUM) = range(12)
 FAMILY_NAMES = {
     CONSTANT: "constant", OSCILLATORY: "oscillatory", PRODUCT_PEAK: "product_peak", CORNER_PEAK: "corner_peak",
     GAUSSIAN: "gaussian", C0: "c0", DISCONTINUOUS: "discontinuous", PRODUCT: "product", NAN_VALUE: "nan",
-    BOX: "box", FUN6: "fun6",
+    BOX: "box", FUN6: "fun6", GAUSSIAN_SUM: "gaussian_sum",
 }
 GENZ_FAMILIES = (OSCILLATORY, PRODUCT_PEAK, CORNER_PEAK, GAUSSIAN, C0, DISCONTINUOUS)
 

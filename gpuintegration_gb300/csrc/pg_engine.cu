@@ -87,6 +87,15 @@ bool ClassifierState::criteria_met(uint64_t n) const {
 }
 
 // ---------------------------------------------------------------------------
+// c^d (1 when c is 0), the constant factor of GAUSSIAN_SUM: d - 1 multiplies
+// in axis order.
+static double gaussian_sum_scale(double c, int d) {
+  if (c == 0.0) return 1.0;
+  double r = c;
+  for (int k = 1; k < d; ++k) r = r * c;
+  return r;
+}
+
 int prepare_desc(const pg_integrand& f, const double* lows, const double* highs, IntegralDesc* out,
                  std::string* why) {
   if (f.ndim < PG_MIN_NDIM || f.ndim > kMaxNdim) {
@@ -108,6 +117,7 @@ int prepare_desc(const pg_integrand& f, const double* lows, const double* highs,
   D.c = f.c;
   D.s0 = 2.0 * 3.14159265358979323846 * f.u[0];
   if (f.family == FAM_FUN6) D.c = 12.0 / (7.0 - 6.0 * std::log(2.0) * std::log(2.0) + std::log(64.0));
+  if (f.family == FAM_GAUSSIAN_SUM) D.s0 = gaussian_sum_scale(f.c, f.ndim);
   D.jac = 1.0;
   int unit = 1;
   for (int k = 0; k < kMaxDim; ++k) {

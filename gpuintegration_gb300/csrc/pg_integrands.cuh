@@ -25,7 +25,8 @@ enum Family : int32_t {
   FAM_NAN = 8,
   FAM_BOX = 9,
   FAM_FUN6 = 10,
-  FAM_COUNT = 11,
+  FAM_GAUSSIAN_SUM = 11,  // exp of the sum of squares; s0 holds c^d (or 1)
+  FAM_COUNT = 12,
   FAM_USER = 64  // a caller's functor (C++ layer); never accepted from a pg_integrand
 };
 
@@ -136,6 +137,17 @@ __device__ __forceinline__ double family_eval(const IntegralDesc& D, const doubl
       return split_product<MAXD>(D, x, true);
     case FAM_PRODUCT:
       return split_product<MAXD>(D, x, false);
+    case FAM_GAUSSIAN_SUM: {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < MAXD; ++i) {
+        if (i < d) {
+          const double q = __dmul_rn(D.a[i], __dsub_rn(x[i], D.u[i]));
+          s = __fma_rn(q, q, s);
+        }
+      }
+      return __dmul_rn(exp(-s), D.s0);
+    }
     case FAM_NAN:
       return __longlong_as_double(0x7ff8000000000000LL);
     case FAM_BOX: {

@@ -55,6 +55,11 @@ typedef enum pg_status {
  *   NAN_VALUE       NaN                                (test/cuda/pagani/NanIntegral.cu:9-16)
  *   BOX             (sum x_i^2)^(c/2)                  (cuda/pagani/demos/function.cuh:113-172)
  *   FUN6            6-D test function of test/cuda/pagani/accuracy_improves_with_epsrel.cu:17-27
+ *   GAUSSIAN_SUM    exp(-sum a_i^2 (x_i - u_i)^2) as one exponential of the sum
+ *                   (squares summed in axis order), times c^d when c != 0: the
+ *                   form of the reference's m-Cubes Gaussian functors
+ *                   (cuda/mcubes/demos/Gauss9D.cu:8-24); one exp per point
+ *                   instead of d, not product-form
  * The product-form families (PRODUCT_PEAK, GAUSSIAN, C0, DISCONTINUOUS,
  * PRODUCT) are evaluated as a product of per-axis factors h_i taken in two
  * halves, (h_0 * ... * h_{m-1}) * (h_m * ... * h_{d-1}) with m = ndim / 2, each
@@ -72,7 +77,8 @@ typedef enum pg_family {
   PG_FAMILY_NAN_VALUE = 8,
   PG_FAMILY_BOX = 9,
   PG_FAMILY_FUN6 = 10,
-  PG_FAMILY_COUNT = 11
+  PG_FAMILY_GAUSSIAN_SUM = 11,
+  PG_FAMILY_COUNT = 12
 } pg_family;
 
 typedef struct pg_integrand {

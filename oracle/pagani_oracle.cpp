@@ -50,6 +50,7 @@ enum Family : int32_t {
   FAM_NAN = 8,
   FAM_BOX = 9,
   FAM_FUN6 = 10,
+  FAM_GAUSSIAN_SUM = 11,
 };
 
 struct Integrand {
@@ -81,6 +82,13 @@ static Prepared prepare(const Integrand& f) {
   p.s0 = 2.0 * 3.14159265358979323846 * f.u[0];
   if (f.family == FAM_FUN6)
     p.c = 12.0 / (7.0 - 6.0 * std::log(2.0) * std::log(2.0) + std::log(64.0));
+  if (f.family == FAM_GAUSSIAN_SUM) {  // c^d, d - 1 multiplies in axis order (1 when c is 0)
+    p.s0 = 1.0;
+    if (f.c != 0.0) {
+      p.s0 = f.c;
+      for (int k = 1; k < f.ndim; ++k) p.s0 = p.s0 * f.c;
+    }
+  }
   return p;
 }
 
@@ -155,6 +163,15 @@ static double eval(const Prepared& p, const double* x) {
       double s = 0.0;
       for (int i = 0; i < d; ++i) s = std::fma(x[i], x[i], s);
       return std::pow(s, 0.5 * p.c);
+    }
+    case FAM_GAUSSIAN_SUM: {
+      // one exponential of the sum of squares (cuda/mcubes/demos/Gauss9D.cu:8-24)
+      double s = 0.0;
+      for (int i = 0; i < d; ++i) {
+        const double q = p.a[i] * (x[i] - p.u[i]);
+        s = std::fma(q, q, s);
+      }
+      return std::exp(-s) * p.s0;
     }
     case FAM_FUN6: {
       // test/cuda/pagani/accuracy_improves_with_epsrel.cu:267-275

@@ -35,6 +35,7 @@ def test_oracle_philox_matches_curand(orc):
     (pg.genz(pg.PRODUCT_PEAK, [3.0, 2.0], [0.4, 0.7]), 1e5),
     (pg.genz(pg.C0, [2.0, 3.0, 1.0, 2.0], [0.5, 0.2, 0.7, 0.4]), 3e5),
     (pg.genz(pg.OSCILLATORY, [1.0, 2.0, 1.5, 0.5, 1.0], [0.1] * 5), 5e5),
+    (pg.genz(pg.GAUSSIAN_SUM, [5.0, 4.0, 3.0, 6.0], [0.3, 0.6, 0.5, 0.45]), 4e5),
 ])
 def test_gpu_matches_oracle(ctx, orc, f, ncall):
     r = ctx.mcubes_integrate(f, 1e-3, 0.0, ncall, titer=12, itmax=8, skip=3, seed=99)

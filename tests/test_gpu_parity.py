@@ -20,7 +20,7 @@ from tests.reference_cases import BOX, CONFIG1, CONFIG1_VALUE, EASY
 pytestmark = pytest.mark.gpu
 
 EXACT_FAMILIES = (pg.CONSTANT, pg.PRODUCT_PEAK, pg.CORNER_PEAK, pg.PRODUCT)
-TRANSC_FAMILIES = (pg.OSCILLATORY, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS)
+TRANSC_FAMILIES = (pg.OSCILLATORY, pg.GAUSSIAN, pg.C0, pg.DISCONTINUOUS, pg.GAUSSIAN_SUM)
 
 
 def _random_integrand(rng, family, d):

@@ -168,3 +168,24 @@ def test_oracle_predict_split_keeps_iteration_15(orc):
     assert r.status == 0 and snap[0] == 16 * 2 ** 15
     left, length = snap[1]
     assert abs(np.prod(length, axis=0).sum() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("d", [2, 4, 6])
+def test_gaussian_sum_family(orc, d):
+    """GAUSSIAN_SUM is the Gaussian family formed as one exponential of the sum of
+    squares, the form of the reference's m-Cubes Gaussian functors
+    (cuda/mcubes/demos/Gauss9D.cu:8-24): pointwise it equals the product form
+    to rounding (1e-12 relative: the sum's rounding scales with its size), and
+    the oracle integrates it to the analytic value."""
+    from gpuintegration_gb300 import workloads as W
+    rng = np.random.default_rng(12 + d)
+    a, u = list(rng.random(d) * 4 + 0.5), list(rng.random(d))
+    fs = pg.Integrand(pg.GAUSSIAN_SUM, d, a, u, c=1.3)
+    fp = pg.Integrand(pg.GAUSSIAN, d, a, u, c=1.3)
+    for _ in range(100):
+        x = rng.random(d)
+        vs, vp = orc.eval_point(fs, x), orc.eval_point(fp, x)
+        assert abs(vs - vp) <= 1e-12 * abs(vp) + 1e-300
+    exact = W.analytic(fs)
+    r, _ = orc.integrate(fs, 1e-6, 0.0)
+    assert r.status == 0 and abs(r.estimate - exact) <= 1e-6 * abs(exact)
