@@ -49,10 +49,38 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k
   }
 }
 
-// Uniform double in (0, 1] from 53 random bits.
+// Exact conversions built from bit patterns on the integer pipe.  The
+// sampling kernel is bound by GB300's FP64 pipe, which also executes the
+// hardware's double<->integer conversions; these give the same values.
+
+// v * 2^shift as a double, for 1 <= v <= 2^53 (exact: v has at most 53
+// significant bits) and a result in the normal range.
+__device__ __forceinline__ double exact_u53_scaled(uint64_t v, int shift) {
+  const int lz = __clzll((long long)v);
+  const uint64_t mant = ((v << lz) << 1) >> 12;  // the bits below the leading one
+  return __longlong_as_double((long long)(((uint64_t)(1023 + 63 - lz + shift) << 52) | mant));
+}
+
+// max(min((int)x, nbins), 1) for a finite x (the bin of a sample), with the
+// comparisons on the bit pattern and the integer part from the exponent and
+// mantissa.
+__device__ __forceinline__ int bin_index(double x, int nbins) {
+  const long long bits = __double_as_longlong(x);
+  if (bits < 0x3ff0000000000000ll) return 1;       // x < 1, negative x included
+  if (bits >= 0x41e0000000000000ll) return nbins;  // x >= 2^31: (int)x saturates
+  const int e = (int)(bits >> 52) - 1023;          // 0..30
+  const int t = (int)(((((unsigned long long)bits << 12) >> 12) | (1ull << 52)) >> (52 - e));
+  return max(min(t, nbins), 1);
+}
+
+// Uniform double in (0, 1] from 53 random bits: (m + 1) * 2^-53.
 __host__ __device__ __forceinline__ double philox_unit(uint32_t a, uint32_t b) {
   const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+#ifdef __CUDA_ARCH__
+  return exact_u53_scaled(m + 1, -53);
+#else
   return (double)(m + 1) * 1.1102230246251565404236316680908203125e-16;  // 2^-53
+#endif
 }
 
 // Device-side state of one m-Cubes run (the weighted mean over iterations,
@@ -142,16 +170,16 @@ __global__ void __launch_bounds__(kMcThreads) mcubes_kernel(McArgs A, Fn fn) {
           }
           const double ran = (j & 1) ? philox_unit(rnd[2], rnd[3]) : philox_unit(rnd[0], rnd[1]);
           // Setup_Integrand_Eval (vegasT.cuh:173-212)
-          const double xn = __fma_rn(__dsub_rn((double)kg[j], ran), A.dxg, 1.0);
-          const int b = max(min((int)xn, A.nbins), 1);
+          const double xn = __fma_rn(__dsub_rn(exact_u53_scaled((uint64_t)kg[j], 0), ran), A.dxg, 1.0);
+          const int b = bin_index(xn, A.nbins);
           const double* xij = sxi + j * nb1;
           double xo, rc;
           if (b > 1) {
             xo = __dsub_rn(xij[b], xij[b - 1]);
-            rc = __fma_rn(__dsub_rn(xn, (double)b), xo, xij[b - 1]);
+            rc = __fma_rn(__dsub_rn(xn, exact_u53_scaled((uint64_t)b, 0)), xo, xij[b - 1]);
           } else {
             xo = xij[b];
-            rc = __dmul_rn(__dsub_rn(xn, (double)b), xo);
+            rc = __dmul_rn(__dsub_rn(xn, 1.0), xo);
           }
           x[j] = __fma_rn(rc, A.dx[j], A.regn[j]);
           wgt = __dmul_rn(wgt, __dmul_rn(xo, A.xnd));
