@@ -36,3 +36,27 @@ def test_serve_overlaps_requests(ctx):
     res, done = ctx.serve(fs, eps, 0.0, arrivals)
     assert all(r.status == 0 for r in res)
     assert done[1:].max() < done[0]
+
+
+@pytest.mark.parametrize("mode", [pg.EVAL_POINTS, pg.EVAL_SET_SUMS])
+def test_served_workload_sample_equals_standalone(ctx, mode):
+    """The served configuration's request stream (Genz integrands, dim 3..10,
+    epsrel log-uniform [1e-6, 1e-3]) on its own Poisson schedule at 2000
+    requests/s, keeping the requests of dimension <= 6 with epsrel >= 1e-5, under
+    a 64 MB region-pool budget so requests queue for admission: every request
+    finishes after it arrives, and each result is its stand-alone result bit for
+    bit."""
+    arrivals_all = W.poisson_arrivals(2000.0, 0.25)
+    cases_all = W.config5_cases(len(arrivals_all))
+    keep = [i for i, c in enumerate(cases_all) if c.integrand.ndim <= 6 and c.epsrel >= 1e-5]
+    assert len(keep) >= 100
+    cases = [cases_all[i] for i in keep]
+    arrivals = arrivals_all[keep]
+    fs = [c.integrand for c in cases]
+    eps = [c.epsrel for c in cases]
+    opt = pg.default_options(eval_mode=mode)
+    served, done = ctx.serve(fs, eps, 0.0, arrivals, budget_bytes=64 << 20, options=opt)
+    assert np.all(done >= arrivals - 1e-6)
+    key = lambda r: (r.estimate, r.errorest, r.nregions, r.status, r.iters, r.neval)  # noqa: E731
+    for f, e, s in zip(fs, eps, served):
+        assert key(s) == key(ctx.integrate(f, e, 0.0, options=pg.default_options(eval_mode=mode)))
