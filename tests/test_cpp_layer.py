@@ -113,6 +113,21 @@ def test_reference_helpers_compile_in_functors(helpers_first):
     assert os.path.getsize(out) > 0
 
 
+def test_helpers_error_behaviour():
+    """Bad tables throw std::invalid_argument before allocating; without a CUDA
+    device the helpers' allocations throw std::bad_alloc; empty tables give NaN
+    (tests/cpp/helpers_errors.cu, run on the host)."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "cpp", "helpers_errors.cu")
+    exe = os.path.join(BUILD, "helpers_errors")
+    subprocess.check_call([_nvcc()] + _flags() + [src, "-o", exe])
+    p = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    print(p.stdout)
+    lines = p.stdout.strip().splitlines()
+    assert p.returncode == 0, p.stdout + p.stderr
+    assert lines and lines[-1].startswith("DONE 0 failures")
+
+
 def test_helpers_header_compiles():
     """include/pagani_gb300_helpers.cuh with the C++ layer: the GPU check program compiles (no GPU needed)."""
     os.makedirs(BUILD, exist_ok=True)
