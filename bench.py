@@ -156,8 +156,9 @@ def _oracle_checked(screen):
     oc = screen.get("oracle_check")
     if not oc:
         return "no candidate (not run)"
-    return (f"{oc['accepted_agree']} of {oc['accepted_checked']} light accepted and "
-            f"{oc['rejected_agree']} of {oc['rejected_checked']} low-dimension rejected candidates")
+    return (f"{oc['accepted_agree']} of {oc['accepted_checked']} accepted candidates with <= {oc['max_regions']} "
+            f"regions and {oc['rejected_agree']} of {oc['rejected_checked']} rejected candidates of dimension <= "
+            f"{oc['max_rejected_dim']}")
 
 
 # ---------------------------------------------------------------------------

@@ -30,8 +30,8 @@ sys.path.insert(0, ROOT)
 from gpuintegration_gb300 import workloads as W  # noqa: E402
 
 PATH = os.path.join(HERE, "config4_screen.json")
-ORACLE_MAX_REGIONS = 20000
-ORACLE_MAX_REJECTED_DIM = 5
+ORACLE_MAX_REGIONS = 200000
+ORACLE_MAX_REJECTED_DIM = 6
 
 
 def main(target=4096, candidates=5600, master=4096):
@@ -96,6 +96,7 @@ def oracle_check():
         rej_ok += not ok
     screen["oracle_check"] = {
         "accepted_checked": acc_n, "accepted_agree": acc_ok, "rejected_checked": rej_n, "rejected_agree": rej_ok,
+        "max_regions": ORACLE_MAX_REGIONS, "max_rejected_dim": ORACLE_MAX_REJECTED_DIM,
         "rule": f"CPU oracle on every accepted candidate with <= {ORACLE_MAX_REGIONS} regions (same decision, "
                 f"region and evaluation counts) and every rejected candidate of dimension <= "
                 f"{ORACLE_MAX_REJECTED_DIM} (rejected too)",

@@ -30,8 +30,8 @@ def cand(screen):
 
 def test_recorded_oracle_check_agrees_everywhere(screen):
     oc = screen["oracle_check"]
-    assert oc["accepted_checked"] >= 3000 and oc["accepted_agree"] == oc["accepted_checked"]
-    assert oc["rejected_checked"] >= 300 and oc["rejected_agree"] == oc["rejected_checked"]
+    assert oc["accepted_checked"] >= 3400 and oc["accepted_agree"] == oc["accepted_checked"]
+    assert oc["rejected_checked"] >= 500 and oc["rejected_agree"] == oc["rejected_checked"]
 
 
 def test_workload_is_the_first_accepted_candidates(screen):
@@ -42,7 +42,7 @@ def test_workload_is_the_first_accepted_candidates(screen):
 
 def test_oracle_repeats_accepted_sample(orc, screen, cand):
     rng = np.random.default_rng(41)
-    light = [k for k, n in enumerate(screen["nregions"]) if n <= S.ORACLE_MAX_REGIONS]
+    light = [k for k, n in enumerate(screen["nregions"]) if n <= 20000]  # a second or two of CPU in all
     for k in rng.choice(light, 200, replace=False):
         ok, r = S.oracle_decision(orc, cand[screen["accepted"][k]])
         assert ok, k

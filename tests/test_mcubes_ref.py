@@ -25,6 +25,11 @@ compared run by run.  Its 6-D Gaussian run is recorded but not compared: its
 weighted mean includes the first, unadapted iterations (no skip), whose
 variance estimates are unreliable for a peak of width 0.01, and it lies 3.2
 standard deviations from the exact value 1.
+
+The 6-D Gaussian's reference runs were recorded with the Gaussian formed as a
+product of per-axis exponentials; the configuration now forms it as one
+exponential of the sum (GAUSSIAN_SUM, as the reference's m-Cubes demos do).
+The function is the same, so the statistical comparison is unchanged.
 """
 import json
 import math
