@@ -11,12 +11,13 @@ which matches the CPU oracle (bit-identical for integrands built from
 
 `python make_config4_screen.py` (needs a GPU) writes
 tests/golden/config4_screen.json.  `python make_config4_screen.py
---oracle-check` (CPU only) repeats the screen's decision with the CPU oracle on
-every candidate the oracle finishes in well under a second -- the accepted
-candidates with at most ORACLE_MAX_REGIONS regions and the rejected
-candidates of dimension at most ORACLE_MAX_REJECTED_DIM -- and records the
-agreement in the file's `oracle_check` entry (tests/test_config4_screen.py
-repeats a seeded sample of it).
+--oracle-check [--max-regions N] [--max-dim D] [--extend]` (CPU only) repeats
+the screen's decision with the CPU oracle on the accepted candidates with at
+most N regions (default ORACLE_MAX_REGIONS) and the rejected candidates of
+dimension at most D (default ORACLE_MAX_REJECTED_DIM), and records the
+agreement in the file's `oracle_check` entry; `--extend` runs only the
+candidates beyond the bounds already recorded and adds them
+(tests/test_config4_screen.py repeats a seeded sample).
 """
 import json
 import os
@@ -74,40 +75,58 @@ def oracle_decision(oracle, case, threads=None):
     return r.status == 0 and W.within_tolerance(r.estimate, case.exact, case.epsrel), r
 
 
-def oracle_check():
+def _record(screen, acc_n, acc_ok, rej_n, rej_ok, max_regions, max_dim, seconds):
+    screen["oracle_check"] = {
+        "accepted_checked": acc_n, "accepted_agree": acc_ok, "rejected_checked": rej_n, "rejected_agree": rej_ok,
+        "max_regions": max_regions, "max_rejected_dim": max_dim,
+        "rule": f"CPU oracle on every accepted candidate with <= {max_regions} regions (same decision, "
+                f"region and evaluation counts) and every rejected candidate of dimension <= {max_dim} "
+                f"(rejected too)",
+        "seconds": round(seconds, 1)}
+    with open(PATH, "w") as f:
+        json.dump(screen, f, separators=(",", ":"))
+
+
+def oracle_check(max_regions=ORACLE_MAX_REGIONS, max_dim=ORACLE_MAX_REJECTED_DIM, extend=False):
+    """Repeats the screen's decisions with the oracle.  With `extend`, only the
+    candidates beyond the bounds already recorded are run and their counts added
+    (the accepted band first, recorded before the rejected band starts)."""
     from oracle import oracle
     oracle.load()
     screen = json.load(open(PATH))
     cand = candidates_of(screen)
+    prev = screen.get("oracle_check") if extend else None
+    lo_regions, lo_dim = (prev["max_regions"], prev["max_rejected_dim"]) if prev else (-1, 0)
+    acc_n, acc_ok, rej_n, rej_ok, secs = ((prev["accepted_checked"], prev["accepted_agree"], prev["rejected_checked"],
+                                           prev["rejected_agree"], prev["seconds"]) if prev else (0, 0, 0, 0, 0.0))
     t0 = time.time()
-    acc_n = acc_ok = 0
     for k, i in enumerate(screen["accepted"]):
-        if screen["nregions"][k] > ORACLE_MAX_REGIONS:
+        if not lo_regions < screen["nregions"][k] <= max_regions:
             continue
         ok, r = oracle_decision(oracle, cand[i])
         acc_n += 1
         acc_ok += ok and r.nregions == screen["nregions"][k] and r.neval == screen["neval"][k]
-    rej_n = rej_ok = 0
+    _record(screen, acc_n, acc_ok, rej_n, rej_ok, max(max_regions, lo_regions), lo_dim, secs + time.time() - t0)
     for i in screen["rejected_before_last"]:
-        if cand[i].integrand.ndim > ORACLE_MAX_REJECTED_DIM:
+        if not lo_dim < cand[i].integrand.ndim <= max_dim:
             continue
         ok, _ = oracle_decision(oracle, cand[i])
         rej_n += 1
         rej_ok += not ok
-    screen["oracle_check"] = {
-        "accepted_checked": acc_n, "accepted_agree": acc_ok, "rejected_checked": rej_n, "rejected_agree": rej_ok,
-        "max_regions": ORACLE_MAX_REGIONS, "max_rejected_dim": ORACLE_MAX_REJECTED_DIM,
-        "rule": f"CPU oracle on every accepted candidate with <= {ORACLE_MAX_REGIONS} regions (same decision, "
-                f"region and evaluation counts) and every rejected candidate of dimension <= "
-                f"{ORACLE_MAX_REJECTED_DIM} (rejected too)",
-        "seconds": round(time.time() - t0, 1)}
-    with open(PATH, "w") as f:
-        json.dump(screen, f, separators=(",", ":"))
+    _record(screen, acc_n, acc_ok, rej_n, rej_ok, max(max_regions, lo_regions), max(max_dim, lo_dim),
+            secs + time.time() - t0)
     print(json.dumps(screen["oracle_check"]))
 
 
 if __name__ == "__main__":
-    if "--oracle-check" in sys.argv[1:]:
-        oracle_check()
+    args = sys.argv[1:]
+    if "--oracle-check" in args:
+        # optional: --max-regions N --max-dim D --extend
+        kw = {}
+        if "--max-regions" in args:
+            kw["max_regions"] = int(args[args.index("--max-regions") + 1])
+        if "--max-dim" in args:
+            kw["max_dim"] = int(args[args.index("--max-dim") + 1])
+        oracle_check(extend="--extend" in args, **kw)
     else:
         main()
